@@ -1,0 +1,431 @@
+"""Benchmark: SpTRSV throughput (GB/s vs the HBM roofline) on one GB300,
+plus time-to-1e-10 of IC0-PCG and of GMRES(30)+ILU0 (FP32 vs FP64
+preconditioner).
+
+Default workload (one "step" = one forward triangular solve):
+  L = IC0 factor of the 3D 7-point Laplacian on a 64^3 grid + 1e-2 I
+  (natural ordering, n = 262,144, nnz(L) = 1,036,288, 190 wavefront
+  levels), 64 right-hand sides ~ N(0,1) in FP64, row-major n x 64.
+The factor is computed on the GPU (the library's IC0).  Inputs are seeded
+synthetic data of the named shape.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbsym|reference]
+
+Under torchrun each rank solves its own replica (the path does not shard
+across GPUs for one system: "replicas only"); value is the sum over ranks
+of the per-rank throughput measured over the max-over-ranks time.
+
+--impl reference times the reference's CPU executor for the same workload
+on the host cores: the oracle's C restatement of sptrsv_csr_levelset
+(one OpenMP parallel-for per level) and of sptrsv_csr with the columns
+spread over threads; the faster is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "sptrsv_gbs"
+UNIT = "GB/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gbsym", choices=["gbsym", "reference"])
+    ap.add_argument("--grid", type=int, default=64)
+    ap.add_argument("--rhs", type=int, default=64)
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--extras-only", action="store_true")
+    return ap.parse_args()
+
+
+def algorithmic_bytes(nnz_l, n, k, vbytes=8, sbytes=8):
+    """(V+4) nnz(L) + 4 (n+1) + 2 S k n: every stored value and index read
+    once, the right-hand sides read once and the solution written once."""
+    return (vbytes + 4) * nnz_l + 4 * (n + 1) + 2 * sbytes * k * n
+
+
+def config(grid, k):
+    return {"workload": "C2 IC0 factor of 3D 7-pt Laplacian %d^3 + 1e-2 I, forward SpTRSV, %d RHS FP64"
+                        % (grid, k),
+            "n": grid ** 3, "rhs": k, "ordering": "natural", "layout": "row-major n x k",
+            "l2": "inputs 2*n*k*8 B; 256 MB L2 flush write between timed steps",
+            "parallelism": "replicas"}
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "1", "yes"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def run_reference(args):
+    world, rank, _ = dist_init()
+    if rank != 0:
+        return
+    import oracle
+    from sympiler_gb300 import matgen as mg
+    orc = oracle.orc()
+    A = mg.lap3d(args.grid, 1e-2)
+    U = mg.triu(A)
+    f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+    L = mg.transpose(mg.CSR(U.n, U.p, U.i, f))
+    nl, lp, ls = orc.build_levelset_csr(L.n, L.p, L.i)
+    k = args.rhs
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(0)
+    sample_cols = max(1, min(k, 8))
+    B = rng.standard_normal((sample_cols, L.n))
+
+    def t_levelset():
+        X = B.copy()
+        t0 = time.perf_counter()
+        orc.sptrsv_csr_levelset_mrhs(L.n, *L.astuple(), X, sample_cols, nl, lp, ls, cores)
+        return (time.perf_counter() - t0) * k / sample_cols
+
+    def t_colpar():
+        X = B.copy()
+        t0 = time.perf_counter()
+        orc.sptrsv_csr_mrhs(L.n, *L.astuple(), X, sample_cols, cores)
+        # columns run in parallel: a sample of c columns on >= c threads
+        # takes one column's time; k columns take ceil(k / threads) rounds
+        dt = time.perf_counter() - t0
+        rounds_sample = -(-sample_cols // cores)
+        return dt / rounds_sample * (-(-k // cores))
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        t_levelset()
+        t_colpar()
+    ts_l, ts_c = [], []
+    for _ in range(args.steps):
+        ts_l.append(t_levelset())
+        ts_c.append(t_colpar())
+    byt = algorithmic_bytes(L.nnz, L.n, k)
+    tl, tc = statistics.median(ts_l), statistics.median(ts_c)
+    best, kind = (tl, "sptrsv_csr_levelset, OpenMP per level") if tl <= tc else \
+        (tc, "sptrsv_csr per column, columns over OpenMP threads")
+    value = byt / best / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": best * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config(args.grid, k),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": "%d of %d RHS columns per step, scaled to %d; best of: levelset "
+                                       "%.1f ms, column-parallel %.1f ms per %d-RHS solve; used: %s"
+                                       % (sample_cols, k, k, tl * 1e3, tc * 1e3, k, kind)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def cpu_baseline_sample(L, k, nl, lp, ls):
+    """Bounded CPU sample of the same workload (oracle port, all host threads)."""
+    import oracle
+    orc = oracle.orc()
+    cores = os.cpu_count() or 1
+    cols = max(1, min(k, 4))
+    B = np.random.default_rng(0).standard_normal((cols, L.n))
+    X = B.copy()
+    orc.sptrsv_csr_levelset_mrhs(L.n, *L.astuple(), X, cols, nl, lp, ls, cores)  # warm
+    reps, t_tot = 0, 0.0
+    while t_tot < 3.0 and reps < 50:
+        X = B.copy()
+        t0 = time.perf_counter()
+        orc.sptrsv_csr_levelset_mrhs(L.n, *L.astuple(), X, cols, nl, lp, ls, cores)
+        t_tot += time.perf_counter() - t0
+        reps += 1
+    t_solve = t_tot / reps * k / cols
+    return {"value": algorithmic_bytes(L.nnz, L.n, k) / t_solve / 1e9, "unit": UNIT, "cores": cores,
+            "kind": "port",
+            "sample": "oracle sptrsv_csr_levelset (OpenMP per level, %d threads), %d RHS columns x %d "
+                      "reps, scaled to %d RHS" % (cores, cols, reps, k)}
+
+
+def load_traffic(workload_key):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(p) as fh:
+            return json.load(fh).get(workload_key)
+    except (OSError, ValueError):
+        return None
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    world, rank, local = dist_init()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+
+    from sympiler_gb300 import matgen as mg
+    from sympiler_gb300 import plans
+    from sympiler_gb300._lib import UPPER_DIAG_FIRST
+    from sympiler_gb300.plans import CsrPlan, TriPlan
+
+    k = args.rhs
+    g = args.grid
+    A = mg.lap3d(g, 1e-2)
+    U = mg.triu(A)
+    # IC0 on the GPU (the library's level-scheduled spic0_csr)
+    vals = torch.from_numpy(U.x.copy()).to(dev)
+    plans.ic0_device(U.n, vals, torch.from_numpy(U.p).to(dev), torch.from_numpy(U.i).to(dev))
+    torch.cuda.synchronize()
+    Lt = mg.CSR(U.n, U.p, U.i, vals.cpu().numpy())
+    L = mg.transpose(Lt)
+    plan = TriPlan(L.n, *L.astuple())
+    info = plan.info()
+    n = L.n
+    byt = algorithmic_bytes(L.nnz, n, k)
+
+    rng = np.random.default_rng(1234 + rank)
+    B = torch.from_numpy(rng.standard_normal((n, k))).to(dev)
+    X = torch.empty_like(B)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+    result = {}
+
+    if not args.extras_only:
+        def step(timed):
+            X.copy_(B)
+            flush.fill_(rank + 1)
+            if timed:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                plan.solve(X)
+                e1.record(stream)
+                return e0, e1
+            plan.solve(X)
+            return None
+
+        for _ in range(max(3, args.warmup)):
+            step(False)
+        torch.cuda.synchronize()
+        sampler = ClockSampler(local)
+        sampler.start()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+        launches0 = plans.kernel_launches()
+        w0 = time.perf_counter()
+        evs = [step(True) for _ in range(args.steps)]
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+        launches = plans.kernel_launches() - launches0
+        if world > 1:
+            torch.distributed.barrier()
+        clocks = sampler.stop()
+        times = [a.elapsed_time(b) / 1e3 for a, b in evs]
+        t_step = sum(times) / len(times)
+        if world > 1:
+            tt = torch.tensor([t_step], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            t_step = float(tt.item())
+        value_rank = byt / t_step / 1e9
+        value = value_rank * world
+
+        # end to end through the C ABI: pinned host buffers, H2D + solve + D2H
+        Hb = torch.empty((n, k), dtype=torch.float64).pin_memory()
+        Hb.copy_(B.cpu())
+        Hx = torch.empty_like(Hb).pin_memory()
+        for _ in range(2):
+            Hx.copy_(Hb)
+            plan.solve_host_ptr(Hx.data_ptr(), k)
+        e2e_t = []
+        for _ in range(max(3, args.steps // 2)):
+            Hx.copy_(Hb)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            plan.solve_host_ptr(Hx.data_ptr(), k)
+            e2e_t.append(time.perf_counter() - t0)
+        e2e_step = statistics.median(e2e_t)
+
+        # parity spot check of the timed result (first column) against a
+        # plain FP64 dense-free check: residual of L x = b on one column
+        x0 = X[:, 0].cpu().numpy()
+        r = L.scipy() @ x0 - B[:, 0].cpu().numpy()
+        resid = float(np.abs(r).max())
+
+        peaks = {}
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+                peaks = json.load(fh)
+        except (OSError, ValueError):
+            pass
+        peak = peaks.get("hbm_gbs")
+        peak_src = "measured" if peak else "fallback"
+        peak = peak or 6800.0
+        traffic = load_traffic("c2_ic0_fwd_%drhs" % k)
+        result.update({
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": dict(config(g, k), levels=info.levels, nnz_L=int(L.nnz),
+                           executor={1: "levelset-graph", 2: "syncfree", 3: "oneblock"}.get(info.exec),
+                           wall_s_timed_region=wall),
+            "roofline": {"bound": "hbm", "achieved": byt / t_step / 1e9, "peak": peak, "unit": "GB/s",
+                         "frac": byt / t_step / 1e9 / peak, "peak_source": peak_src,
+                         "traffic": traffic,
+                         "algorithmic_bytes_per_solve": byt,
+                         "note": "one launch = one forward solve (graph of per-level kernels); "
+                                 "duration from CUDA events on the launch stream"},
+            "e2e": {"value": byt / e2e_step / 1e9, "unit": UNIT, "h2d_bytes_per_step": n * k * 8,
+                    "d2h_bytes_per_step": n * k * 8, "ms_per_step": e2e_step * 1e3,
+                    "api": "gbsym_tri_solve_host (pinned host x, row-major)"},
+            "gpu_launches": int(launches),
+            "clocks": clocks,
+            "check": {"max_abs_residual_col0": resid},
+        })
+
+    if rank == 0 and not args.no_extras:
+        extras = {}
+        # 1-RHS forward solve on the same factor
+        x1 = B[:, 0].contiguous()
+        x1w = torch.empty_like(x1)
+        for _ in range(3):
+            x1w.copy_(x1)
+            plan.solve(x1w)
+        ts = []
+        for _ in range(10):
+            x1w.copy_(x1)
+            flush.fill_(3)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            plan.solve(x1w)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        t1 = statistics.median(ts)
+        b1 = algorithmic_bytes(L.nnz, n, 1)
+        extras["sptrsv_1rhs"] = {"us": t1 * 1e6, "gbs": b1 / t1 / 1e9, "levels": info.levels,
+                                 "us_per_level": t1 * 1e6 / info.levels}
+        # IC0-PCG to 1e-10 on C2 (FP64 throughout)
+        Pt = TriPlan(n, *Lt.astuple(), kind=UPPER_DIAG_FIRST)
+        Ac = CsrPlan(n, *A.astuple())
+        xs = np.random.default_rng(7).standard_normal(n)
+        bb = torch.from_numpy(A.scipy() @ xs).to(dev)
+        xx = torch.zeros(n, dtype=torch.float64, device=dev)
+        plans.pcg(Ac, plan, Pt, bb, xx, tol=1e-10, maxit=2000)
+        xx.zero_()
+        res = plans.pcg(Ac, plan, Pt, bb, xx, tol=1e-10, maxit=2000)
+        extras["pcg_c2"] = {"seconds": res.seconds, "iterations": res.iterations, "relres": res.relres,
+                            "err_vs_xstar": float(np.linalg.norm(xx.cpu().numpy() - xs) / np.linalg.norm(xs))}
+        # GMRES(30) + right ILU0 on the 96^3 convection-diffusion operator
+        from sympiler_gb300._lib import ILU_UNIT_LOWER, ILU_UPPER
+        C = mg.convdiff3d(96)
+        d = mg.diag_ptr(C)
+        dC = [torch.from_numpy(a).to(dev) for a in (C.p, C.i, C.x, d)]
+        lu = torch.empty(C.nnz, dtype=torch.float64, device=dev)
+        plans.ilu0_device(C.n, *dC, lu)
+        Cp = CsrPlan(C.n, dC[0], dC[1], dC[2])
+        bc = torch.from_numpy(np.random.default_rng(9).uniform(-1, 1, C.n)).to(dev)
+        out = {}
+        for prec in ("f32", "f64"):
+            Lu = TriPlan(C.n, dC[0], dC[1], lu, kind=ILU_UNIT_LOWER, diags=dC[3], dtype=prec)
+            Up = TriPlan(C.n, dC[0], dC[1], lu, kind=ILU_UPPER, diags=dC[3], dtype=prec)
+            xg = torch.zeros(C.n, dtype=torch.float64, device=dev)
+            plans.gmres(Cp, Lu, Up, bc, xg, mr=30, maxit=100, tol=1e-10)
+            runs = []
+            for _ in range(2):
+                xg.zero_()
+                runs.append(plans.gmres(Cp, Lu, Up, bc, xg, mr=30, maxit=100, tol=1e-10))
+            best = min(runs, key=lambda r: r.seconds)
+            out[prec] = {"seconds": best.seconds, "iterations": best.iterations, "restarts": best.restarts,
+                         "relres": best.relres, "status": best.status}
+        out["speedup_fp32_precond"] = out["f64"]["seconds"] / out["f32"]["seconds"]
+        extras["gmres_c3"] = out
+        result["extras"] = extras
+    if rank == 0:
+        if not args.extras_only:
+            try:
+                import oracle  # noqa: F401  (CPU baseline leg only)
+                o = oracle.orc()
+                nl, lp, ls = o.build_levelset_csr(L.n, L.p, L.i)
+                result["cpu_baseline"] = cpu_baseline_sample(L, k, nl, lp, ls)
+            except Exception as ex:  # the baseline must not hide the GPU number
+                result["cpu_baseline"] = {"value": None, "unit": UNIT, "error": str(ex)}
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,296 @@
+/*
+ * gbsym.h -- C ABI of the GB300 sparse triangular-solve executor.
+ *
+ * Two layers:
+ *
+ *  1. Drop-ins.  One `gbsym_*` function per reference function on the
+ *     triangular-solve path of sympiler/sympiler, with the reference's
+ *     argument list, argument meaning and in-place behaviour.  All arrays are
+ *     caller-owned HOST memory; the call uploads, runs on the current CUDA
+ *     device, downloads and returns when the result is in the caller's
+ *     buffer.  `void` drop-ins record their status for gbsym_last_error();
+ *     they never abort.  The reference function each one replaces is cited
+ *     beside it (paths inside the sympiler source tree).
+ *
+ *  2. Plans.  Device-resident operators (level-packed triangles, CSR
+ *     matrices) built once and applied many times on a caller stream, with
+ *     device pointers; the Krylov drivers, the adjoint and the batched
+ *     executor sit on top of them.  A `void *stream` argument is a
+ *     cudaStream_t; NULL means the CUDA default (legacy) stream.
+ *
+ * Conventions shared with the reference:
+ *   - int32 CSR/CSC arrays; lower-triangular CSR has the diagonal LAST in
+ *     each row, lower-triangular CSC has it FIRST in each column;
+ *   - the right-hand side is passed in x and overwritten by the solution;
+ *   - multi-RHS arrays are column-major n x k (x[i + j*n]), as in
+ *     SolverSettings::solve_only (sparse_blas/parsy/cholesky_solver.cpp:
+ *     805-813); plans also accept row-major n x k (x[i*k + j]), which is the
+ *     layout the executor computes in.
+ *
+ * Floating point: every row of every solve and product is accumulated in
+ * the reference's storage order with separately rounded multiply and
+ * subtract (no fused multiply-add), so FP64 results are bit-identical to
+ * the reference compiled without floating-point contraction, for rows with
+ * at most GBSYM_EXACT_ROW_MAX off-diagonal entries.  Longer rows use
+ * warp-cooperative partial sums (relative difference ~1e-15).
+ */
+#ifndef GBSYM_H
+#define GBSYM_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status ------------------------------------------------------------ */
+enum gbsym_status {
+  GBSYM_OK = 0,
+  GBSYM_ERR_NULL_ARG = 1,      /* a required pointer is NULL               */
+  GBSYM_ERR_BAD_SCHEDULE = 2,  /* level/partition arrays violate the DAG   */
+  GBSYM_ERR_PIVOT = 3,         /* zero/non-positive pivot in a factor      */
+  GBSYM_ERR_TIMEOUT = 4,       /* a bounded device wait gave up            */
+  GBSYM_ERR_CUDA = 5,          /* a CUDA runtime call failed               */
+  GBSYM_ERR_BAD_MATRIX = 6,    /* malformed CSR/CSC (bounds, diagonal)     */
+  GBSYM_ERR_SIZE = 7,          /* size argument out of range               */
+  GBSYM_ERR_NOT_CONVERGED = 8, /* Krylov driver hit its iteration limit    */
+  GBSYM_ERR_UNSUPPORTED = 9    /* option combination not implemented       */
+};
+
+#define GBSYM_EXACT_ROW_MAX 4096
+
+/* Status of the most recent drop-in call on this host thread. */
+int gbsym_last_error(void);
+const char *gbsym_status_string(int status);
+/* Host buffers returned by the schedule builders; release with gbsym_free. */
+void gbsym_free(void *p);
+/* Number of kernels this library has launched in this process so far. */
+unsigned long long gbsym_kernel_launches(void);
+
+/* ---- drop-ins: SpTRSV, CSR row-pull ------------------------------------- */
+/* sparse_blas/sptrsv.cpp:17-25 ; include/sympiler/sparse_blas_lib.h:126-127 */
+void gbsym_sptrsv_csr(int n, int *Lp, int *Li, double *Lx, double *x);
+/* sparse_blas/sptrsv.cpp:28-37 ; sparse_blas_lib.h:137 (unit lower, no divide) */
+void gbsym_sptrsv_csr_ilu(int n, const int *Lp, const int *Li, const double *Lx,
+                          const int *diags, double *x);
+/* sparse_blas/sptrsv.cpp:109-127 ; sparse_blas_lib.h:139-141 (divides by Lx[diags[i]]) */
+void gbsym_sptrsv_csr_ilu_lbc(int n, const int *Lp, const int *Li,
+                              const double *Lx, const int *diags, double *x,
+                              const int level_no, const int *level_ptr,
+                              const int *par_ptr, const int *partition);
+/* sparse_blas/sptrsv.cpp:40-55 ; sparse_blas_lib.h:146-148 */
+void gbsym_sptrsv_csr_levelset(int n, const int *Lp, const int *Li,
+                               const double *Lx, double *x, int levels,
+                               const int *levelPtr, const int *levelSet);
+/* sparse_blas/sptrsv.cpp:57-76 ; sparse_blas_lib.h:151-153 */
+void gbsym_sptrsv_csr_lbc(int n, int *Lp, int *Li, double *Lx, double *x,
+                          int level_no, int *level_ptr, int *par_ptr,
+                          int *partition);
+/* sparse_blas/sptrsv.cpp:78-107 ; sparse_blas_lib.h:157-161.  tmp is the
+ * reference's per-thread scratch; it is not read and not written here. */
+void gbsym_sptrsv_csr_lbc_redundant(int n, int *Lp, int *Li, double *Lx,
+                                    double *x, double *b, int level_no,
+                                    int *level_ptr, int *par_ptr,
+                                    int *partition, double *tmp);
+
+/* ---- drop-ins: SpTRSV, CSC ---------------------------------------------- */
+/* sparse_blas/sptrsv.cpp:129-137 ; sparse_blas_lib.h:170 */
+void gbsym_sptrsv_csc(int n, int *Lp, int *Li, double *Lx, double *x);
+/* sparse_blas/sptrsv.cpp:139-156 ; sparse_blas_lib.h:174-175 */
+void gbsym_sptrsv_csc_levelset(int n, int *Lp, int *Li, double *Lx, double *x,
+                               int levels, const int *levelptr,
+                               const int *levelset);
+/* sparse_blas/sptrsv.cpp:158-174 ; sparse_blas_lib.h:177-178 */
+void gbsym_sptrsv_csc_lbc(int n, int *Lp, int *Li, double *Lx, double *x,
+                          int level_no, int *level_ptr, int *par_ptr,
+                          int *partition);
+/* sparse_blas/sptrsv_lt.cpp:11-20 ; sparse_blas_lib.h:330.  L^T x = b on the
+ * CSC of L.  Returns 0 on NULL input, 1 on success (as the reference). */
+int gbsym_ltsolve(int n, int *Lp, int *Li, double *Lx, double *x);
+/* sparse_blas/parsy/triangularSolve/Triangular_CSC.cpp:18-28, 30-40, 57-76,
+ * 78-101 ; include/sympiler/parsy/triangularSolve/Triangular_CSC.h */
+int gbsym_parsy_lsolve(int n, int *Lp, int *Li, double *Lx, double *x);
+int gbsym_parsy_ltsolve(int n, int *Lp, int *Li, double *Lx, double *x);
+int gbsym_parsy_lsolvePar(int n, int *Lp, int *Li, double *Lx, double *x,
+                          int levels, int *levelPtr, int *levelSet, int chunk);
+int gbsym_parsy_lsolveParH2(int n, int *Lp, int *Li, double *Lx, double *x,
+                            int levels, int *levelPtr, int *levelSet,
+                            int parts, int *parPtr, int *partition, int chunk);
+
+/* ---- drop-ins: SpMV ------------------------------------------------------ */
+/* sparse_blas/spmv.cpp:12-21 ; sparse_blas_lib.h:19-20 */
+void gbsym_spmv_csr(int n, const int *Ap, const int *Ai, const double *Ax,
+                    const double *x, double *y);
+/* sparse_blas/spmv.cpp:23-34 ; sparse_blas_lib.h:32-33.  z += A x (z is NOT
+ * cleared), then z = a z + b y. */
+void gbsym_spmv_csr_axpby(int n, const int *Ap, const int *Ai, const double *Ax,
+                          const double *x, const double *y, double *z,
+                          double a, double b);
+/* sparse_blas/spmv.cpp:37-57 ; sparse_blas_lib.h:36-37 */
+void gbsym_spmv_csr_parallel(int n, const int *Ap, const int *Ai,
+                             const double *Ax, const double *x, double *y);
+
+/* ---- drop-ins: factor producers and the ILU apply ----------------------- */
+/* sparse_blas/spilu0.cpp:11-51 ; sparse_blas_lib.h:276-277 */
+void gbsym_spilu0_csr(int n, int nnz, const int *Ap, const int *Ai,
+                      const double *Ax, const int *A_diag, double *l);
+/* sparse_blas/spic0.cpp:106-128 ; sparse_blas_lib.h:242 (upper CSR of A, in place) */
+void gbsym_spic0_csr(int n, double *val, int *rowPtr, int *rowIdx);
+/* sparse_blas/parsy/gmres/mgmres.cpp:598-689 ; include/sympiler/parsy/gmres/mgmres.hpp:41 */
+void gbsym_parsy_lus_cr(int n, int nz_num, int *ia, int *ja, double *l,
+                        int *ua, double *r, double *z);
+
+/* ---- drop-ins: schedule builders ---------------------------------------- */
+/* Replaces build_levelSet_CSC of the reference's `aggregation` dependency
+ * (call sites Catch_tests/sptrsv_tests.cpp:59, demo/sptrsv_demo_utils.h:
+ * 42-45).  Computed on the GPU.  level(i) = 0 without off-diagonals, else
+ * 1 + max level of its dependencies; rows ascending inside each level.
+ * *level_ptr (level_no+1 ints) and *level_set (n ints) are allocated here;
+ * release them with gbsym_free.  Returns level_no, or -status on error. */
+int gbsym_build_levelset_csc(int n, const int *Lp, const int *Li,
+                             int **level_ptr, int **level_set);
+/* The same DAG read from the CSR of L (diagonal last). */
+int gbsym_build_levelset_csr(int n, const int *Lp, const int *Li,
+                             int **level_ptr, int **level_set);
+/* Level set of the backward solve on an upper CSR (diagonal first). */
+int gbsym_build_levelset_upper_csr(int n, const int *Up, const int *Ui,
+                                   int **level_ptr, int **level_set);
+
+/* ======================================================================== */
+/* Plans (device-resident).                                                 */
+/* ======================================================================== */
+
+/* How a stored row defines a triangular row of the solve. */
+enum gbsym_tri_kind {
+  GBSYM_LOWER_DIAG_LAST = 0,  /* CSR of L: off-diagonals then the diagonal  */
+  GBSYM_UPPER_DIAG_FIRST = 1, /* CSC of L read as CSR of L^T (ltsolve), or
+                                 the CSR of an upper triangle              */
+  GBSYM_ILU_UNIT_LOWER = 2,   /* [p[i], diags[i]), no division            */
+  GBSYM_ILU_UPPER = 3,        /* (diags[i], p[i+1]), divide by diagonal   */
+  GBSYM_ILU_LOWER_DIV = 4     /* [p[i], diags[i]), divide by l[diags[i]]  */
+};
+enum gbsym_dtype { GBSYM_F64 = 0, GBSYM_F32 = 1 };
+enum gbsym_layout { GBSYM_COL_MAJOR = 0, GBSYM_ROW_MAJOR = 1 };
+enum gbsym_exec {
+  GBSYM_EXEC_AUTO = 0,      /* autotuner choice                            */
+  GBSYM_EXEC_LEVELSET = 1,  /* one launch per level, captured in a graph   */
+  GBSYM_EXEC_SYNCFREE = 2,  /* one persistent launch, per-row ready flags  */
+  GBSYM_EXEC_ONEBLOCK = 3   /* one thread block sweeps all levels          */
+};
+
+typedef struct gbsym_tri_s *gbsym_tri;
+
+typedef struct {
+  int n;
+  int levels;          /* wavefront depth                                  */
+  long long nnz_off;   /* stored off-diagonal entries                      */
+  int dtype;           /* GBSYM_F64 / GBSYM_F32 value storage              */
+  int exec;            /* executor chosen for k = 1                        */
+  int max_level_rows;  /* widest level                                     */
+  long long bytes_matrix; /* device bytes of the packed triangle           */
+} gbsym_tri_info;
+
+/* Build a level-packed triangle from a stored matrix.
+ * p/i/x/diags may be host (on_device = 0) or device (on_device = 1)
+ * pointers; diags is needed for the GBSYM_ILU_* kinds only.  level_ptr /
+ * level_set may be NULL (the schedule is built on the GPU) or a level
+ * schedule to execute (validated first: GBSYM_ERR_BAD_SCHEDULE).
+ * value_dtype chooses FP64 or FP32 storage of the packed values (x is
+ * always FP64 on input; FP32 storage rounds it once). */
+int gbsym_tri_create(gbsym_tri *out, int n, const int *p, const int *i,
+                     const double *x, const int *diags, int kind,
+                     int value_dtype, int on_device, const int *level_ptr,
+                     const int *level_set, int levels, void *stream);
+int gbsym_tri_destroy(gbsym_tri t);
+int gbsym_tri_get_info(gbsym_tri t, gbsym_tri_info *info);
+/* Force an executor (GBSYM_EXEC_*); AUTO restores the autotuned choice. */
+int gbsym_tri_set_exec(gbsym_tri t, int exec);
+/* Copy the schedule into host buffers of levels+1 and n ints. */
+int gbsym_tri_get_schedule(gbsym_tri t, int *level_ptr, int *level_set);
+
+/* Solve in place on device memory: x holds k right-hand sides in the given
+ * layout and dtype (FP64 or FP32 vectors).  An FP32 solve requires FP32
+ * value storage; an FP64 solve accepts either.  Stream-ordered. */
+int gbsym_tri_solve(gbsym_tri t, void *x, int k, int layout, int dtype,
+                    void *stream);
+/* The lbc_redundant row formula: x_i = ((0 - sum_j L_ij x_j) + b_i)/L_ii. */
+int gbsym_tri_solve_b(gbsym_tri t, const double *b, double *x, void *stream);
+/* End-to-end: x is HOST memory (pinned or pageable), copied in, solved and
+ * copied back before the call returns. */
+int gbsym_tri_solve_host(gbsym_tri t, double *x, int k, int layout);
+
+/* ---- CSR matrix plan (SpMV) -------------------------------------------- */
+typedef struct gbsym_csr_s *gbsym_csr;
+int gbsym_csr_create(gbsym_csr *out, int n, int ncols, const int *p,
+                     const int *i, const double *x, int value_dtype,
+                     int on_device, void *stream);
+int gbsym_csr_destroy(gbsym_csr a);
+/* y = A x  (FP64 or FP32 vectors matching the stored dtype). */
+int gbsym_csr_spmv(gbsym_csr a, const void *x, void *y, int dtype, void *stream);
+/* z = alpha (z + A x) + beta y, the reference's accumulate form. */
+int gbsym_csr_spmv_axpby(gbsym_csr a, const double *x, const double *y,
+                         double *z, double alpha, double beta, void *stream);
+
+/* ---- GPU factorisations on device plans --------------------------------- */
+/* ILU0 of a CSR with sorted columns and a diagonal in every row: returns in
+ * l_dev (device, nnz doubles) the packed factor of spilu0_csr.
+ * All pointers are device pointers. */
+int gbsym_ilu0_device(int n, const int *Ap, const int *Ai, const double *Ax,
+                      const int *A_diag, double *l, void *stream);
+/* IC0 (spic0_csr) in place on the device copy of the upper CSR of A. */
+int gbsym_ic0_device(int n, double *val, const int *rowPtr, const int *rowIdx,
+                     void *stream);
+
+/* ---- Krylov drivers (device vectors) ------------------------------------ */
+typedef struct {
+  int iterations;       /* PCG iterations / GMRES inner steps              */
+  int restarts;         /* GMRES outer cycles                              */
+  double relres;        /* final ||b - A x|| / ||b|| computed in FP64       */
+  double seconds;       /* wall time of the solve, device-synchronised     */
+  int status;
+} gbsym_krylov_result;
+
+/* IC0-preconditioned CG.  L is the plan of the forward solve (lower CSR of
+ * the factor), Lt the plan of the transposed solve (its CSC as an upper
+ * CSR).  b, x are device FP64 vectors; x holds the initial guess. */
+int gbsym_pcg(gbsym_csr A, gbsym_tri L, gbsym_tri Lt, const double *b,
+              double *x, double tol, int maxit, gbsym_krylov_result *res,
+              void *stream);
+/* Right-preconditioned GMRES(mr) with ILU0: Lu = unit-lower plan, U = upper
+ * plan of the same packed factor.  The preconditioner runs in the dtype
+ * the two plans store (FP32 or FP64); SpMV, Arnoldi, Givens and the
+ * residual are FP64. */
+int gbsym_gmres(gbsym_csr A, gbsym_tri Lu, gbsym_tri U, const double *b,
+                double *x, int mr, int maxit, double tol,
+                gbsym_krylov_result *res, void *stream);
+
+/* ---- adjoint of the triangular solve ------------------------------------ */
+/* Given X = L^{-1} B (row-major n x k, device) and G = dloss/dX, computes
+ * G_B = L^{-T} G in place in g (Lt = plan of L^T, i.e. the CSC of L as an
+ * upper CSR) and the gradient on L's stored values,
+ * grad[p] = -sum_r G_B[row(p), r] * X[col(p), r], for every stored entry p
+ * of the CSR of L (the diagonal included: grad = -sum_r G_B[i,r] X[i,r]).
+ * Lp/Li are the device CSR arrays of L (diagonal last). */
+int gbsym_tri_adjoint(gbsym_tri Lt, int n, const int *Lp, const int *Li,
+                      const double *X, double *g, int k, double *grad,
+                      void *stream);
+
+/* ---- batched uneven systems --------------------------------------------- */
+typedef struct gbsym_batch_s *gbsym_batch;
+/* nsys lower triangles (CSR, diagonal last) given as host arrays of host
+ * pointers; all are packed into one device pool and solved by one
+ * persistent launch over (system, level) work items. */
+int gbsym_batch_create(gbsym_batch *out, int nsys, const int *n,
+                       const int *const *Lp, const int *const *Li,
+                       const double *const *Lx, int value_dtype, void *stream);
+int gbsym_batch_destroy(gbsym_batch b);
+/* x: device, concatenation of the systems' row-major n_s x k blocks (FP64
+ * or FP32).  offsets (host, nsys+1) receives the row offset of each system
+ * when non-NULL. */
+int gbsym_batch_solve(gbsym_batch b, void *x, int k, int dtype, void *stream);
+int gbsym_batch_row_offsets(gbsym_batch b, long long *offsets);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,118 @@
+// tri.cuh -- the level-packed triangle (gbsym_tri) shared by the solve,
+// Krylov, adjoint and batched translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <vector>
+
+#include "common.cuh"
+
+namespace gbsym {
+
+// Device view of a level-packed triangle.  Packed row k is original row
+// perm[k]; its off-diagonal entries are ci/val[rp[k] .. rp[k+1]) in the
+// caller's storage order (column indices stay in the ORIGINAL numbering, so
+// x is addressed in the caller's order); dg[k] is its divisor, or dg is
+// null for a unit triangle.  Rows of level l occupy packed positions
+// lev_ptr[l] .. lev_ptr[l+1].
+template <class T>
+struct TriView {
+  const int *__restrict__ perm;
+  const int *__restrict__ rp;
+  const int *__restrict__ ci;
+  const T *__restrict__ val;
+  const T *__restrict__ dg;
+};
+
+// Internal kinds used only by the schedule builders: every stored entry on
+// the dependency side of the diagonal is a dependency, wherever it sits in
+// the row, and the diagonal need not be present.
+constexpr int kKindStrictLower = 100;
+constexpr int kKindStrictUpper = 101;
+
+inline bool kind_is_upper(int kind) {
+  return kind == GBSYM_UPPER_DIAG_FIRST || kind == GBSYM_ILU_UPPER || kind == kKindStrictUpper;
+}
+inline bool kind_is_unit(int kind) { return kind == GBSYM_ILU_UNIT_LOWER; }
+
+struct GraphEntry {
+  const void *x = nullptr;
+  const void *b = nullptr;
+  int k = 0, dtype = 0, exec = 0;
+  cudaGraphExec_t exec_graph = nullptr;
+  unsigned long long nodes = 0;
+  unsigned long long stamp = 0;
+};
+
+}  // namespace gbsym
+
+struct gbsym_tri_s {
+  int n = 0;
+  int nlev = 0;
+  int kind = 0;
+  int vdtype = GBSYM_F64;
+  long long nnz_off = 0;
+  int max_level_rows = 0;
+  int exec = GBSYM_EXEC_LEVELSET;  // autotuned
+  int exec_forced = GBSYM_EXEC_AUTO;
+  std::vector<int> h_lev_ptr;        // packed level boundaries (host copy)
+  gbsym::DBuf<int> lev_ptr, perm, rp, ci;
+  gbsym::DBuf<double> val64, dg64;
+  gbsym::DBuf<float> val32, dg32;
+  gbsym::DBuf<int> err;              // device error word(s)
+  gbsym::DBuf<int> flags;            // sync-free ready flags (per packed row)
+  gbsym::DBuf<int> ticket;           // sync-free work counter
+  int epoch = 0;                     // sync-free flag generation
+  gbsym::DBuf<char> scratch;         // layout-conversion scratch
+  gbsym::DBuf<char> io;              // device copy for host-memory solves
+  cudaStream_t cap_stream = nullptr; // private stream for graph capture
+  std::vector<gbsym::GraphEntry> graphs;
+  unsigned long long graph_clock = 0;
+
+  gbsym::TriView<double> view64() const {
+    return {perm.p, rp.p, ci.p, val64.p, kind == GBSYM_ILU_UNIT_LOWER ? nullptr : dg64.p};
+  }
+  gbsym::TriView<float> view32() const {
+    return {perm.p, rp.p, ci.p, val32.p, kind == GBSYM_ILU_UNIT_LOWER ? nullptr : dg32.p};
+  }
+  ~gbsym_tri_s();
+};
+
+namespace gbsym {
+// Solve on device memory, row-major n x k (k >= 1), in place.  b non-null
+// selects the "redundant" row formula (k == 1, FP64 only).
+void tri_solve_rowmajor(gbsym_tri_s *t, void *x, const void *b, int k, int dtype,
+                        cudaStream_t s);
+// Build a plan from device arrays (validates matrix and schedule).
+gbsym_tri_s *tri_build(int n, const int *d_p, const int *d_i, const double *d_x,
+                       const int *d_diags, int kind, int vdtype,
+                       const int *h_level_ptr, const int *d_level_set, int levels,
+                       cudaStream_t s);
+// Sync-free level computation on device arrays: returns the level count,
+// fills d_level_ptr (levels+1) and d_level_set (n).  Used by the plan and
+// by the schedule-builder drop-ins.
+int build_levels_device(int n, const int *d_p, const int *d_i, const int *d_diags,
+                        int kind, DBuf<int> &d_level_ptr, DBuf<int> &d_level_set,
+                        cudaStream_t s);
+// Transpose of a square CSR pattern: for every entry e (row r, col c) of the
+// input, output row c lists (col r, src e) with r ascending.
+struct Transposed {
+  DBuf<int> rp, ci, src;
+};
+void transpose_pattern(int n, int nnz, const int *p, const int *ci, Transposed &out,
+                       cudaStream_t s);
+// Incomplete factorisations on device arrays (factor.cu).
+void ilu0_device(int n, const int *Ap, const int *Ai, const double *Ax, const int *A_diag,
+                 double *l, cudaStream_t s);
+void ic0_device(int n, double *val, const int *up, const int *ui, cudaStream_t s);
+// Checks that (p, i, diags) is a well-formed triangle of the given kind.
+void validate_matrix(int n, const int *d_p, const int *d_i, const int *d_diags,
+                     int kind, cudaStream_t s);
+// Checks an LBC schedule (coarse levels -> partitions -> rows) against the
+// DAG of the triangle: every dependency of a row lies in an earlier coarse
+// level or earlier in the same partition.
+void validate_lbc(int n, const int *d_p, const int *d_i, const int *d_diags, int kind,
+                  int level_no, const int *h_level_ptr, const int *h_par_ptr,
+                  const int *h_partition, cudaStream_t s);
+}  // namespace gbsym

@@ -1,0 +1,219 @@
+"""Seeded synthetic matrices for the SpTRSV / Krylov workloads.
+
+The reference benchmarks its executors on SuiteSparse matrices and on random
+lower-triangular patterns; neither travels here, so these generators build
+the named stencil operators directly, in natural (lexicographic, x fastest)
+ordering, as CSR with ascending column indices:
+
+* ``lap2d(nx, ny)``            -- 5-point Laplacian, diagonal 4, off-diagonals -1.
+* ``lap3d(g, shift)``          -- 7-point Laplacian on g^3, diagonal 6+shift.
+* ``convdiff3d(g, vel, peclet)`` -- 7-point diffusion plus first-order upwind
+  convection, scaled by h^2/nu: off-diagonal -1 (downwind side) and
+  -1 - c_d (upwind side), diagonal 6 + sum_d |c_d|, with
+  c_d = 2 * peclet * vhat_d (cell Peclet number |v| h / (2 nu)).
+* ``aniso_poisson2d(g, eps, sigma, rng)`` -- cell-centred finite volumes for
+  -d/dx(a du/dx) - eps d/dy(a du/dy), log-normal cell coefficients
+  a = exp(sigma N(0,1)), harmonic face means, Dirichlet walls.
+* ``random_spd(n, nnz_per_row, rng)`` -- symmetric pattern with N(0,1)
+  off-diagonals, made strictly diagonally dominant.
+* ``random_lower(n, density, rng)`` -- random lower triangle with a
+  dominant diagonal (the reference's random_square_sparse + make_half test
+  inputs are not available; this stands in for their shape).
+
+All return ``CSR`` tuples (n, indptr int32, indices int32, data float64).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+import scipy.sparse as sp
+
+
+@dataclass
+class CSR:
+    n: int
+    p: np.ndarray  # int32[n+1]
+    i: np.ndarray  # int32[nnz]
+    x: np.ndarray  # float64[nnz]
+
+    @property
+    def nnz(self) -> int:
+        return int(self.p[self.n])
+
+    def astuple(self):
+        return self.p, self.i, self.x
+
+    def scipy(self):
+        return sp.csr_matrix((self.x, self.i, self.p), shape=(self.n, self.n))
+
+
+def from_scipy(m) -> CSR:
+    m = sp.csr_matrix(m)
+    m.sum_duplicates()
+    m.sort_indices()
+    return CSR(m.shape[0], np.ascontiguousarray(m.indptr, dtype=np.int32),
+               np.ascontiguousarray(m.indices, dtype=np.int32),
+               np.ascontiguousarray(m.data, dtype=np.float64))
+
+
+def _stencil(shape, center, offs):
+    """Assemble a constant-coefficient stencil on a lexicographic grid.
+
+    ``offs`` is a list of (axis, step, value) with step = +-1.
+    """
+    dims = list(shape)
+    n = int(np.prod(dims))
+    idx = np.arange(n, dtype=np.int64)
+    coords = []
+    rem = idx.copy()
+    for d in dims:
+        coords.append(rem % d)
+        rem //= d
+    rows = [idx]
+    cols = [idx]
+    vals = [np.full(n, center, dtype=np.float64)]
+    stride = 1
+    strides = []
+    for d in dims:
+        strides.append(stride)
+        stride *= d
+    for axis, step, value in offs:
+        c = coords[axis]
+        ok = (c + step >= 0) & (c + step < dims[axis])
+        r = idx[ok]
+        rows.append(r)
+        cols.append(r + step * strides[axis])
+        vals.append(np.full(r.size, value, dtype=np.float64))
+    m = sp.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(n, n))
+    return from_scipy(m)
+
+
+def lap2d(nx: int, ny: int | None = None) -> CSR:
+    ny = nx if ny is None else ny
+    return _stencil((nx, ny), 4.0, [(0, -1, -1.0), (0, 1, -1.0), (1, -1, -1.0), (1, 1, -1.0)])
+
+
+def lap3d(g: int, shift: float = 0.0) -> CSR:
+    offs = [(a, s, -1.0) for a in range(3) for s in (-1, 1)]
+    return _stencil((g, g, g), 6.0 + shift, offs)
+
+
+def convdiff3d(g: int, vel=(1.0, 0.5, 0.25), peclet: float = 0.5) -> CSR:
+    v = np.asarray(vel, dtype=np.float64)
+    vhat = v / np.linalg.norm(v)
+    c = 2.0 * peclet * vhat
+    offs = []
+    for a in range(3):
+        up = -1 if c[a] >= 0 else 1          # upwind neighbour
+        offs.append((a, up, -1.0 - abs(c[a])))
+        offs.append((a, -up, -1.0))
+    return _stencil((g, g, g), 6.0 + float(np.abs(c).sum()), offs)
+
+
+def aniso_poisson2d(g: int, eps: float = 0.01, sigma: float = 1.0,
+                    rng: np.random.Generator | None = None) -> CSR:
+    rng = np.random.default_rng(0) if rng is None else rng
+    a = np.exp(sigma * rng.standard_normal((g, g)))  # a[y, x]
+    n = g * g
+    idx = np.arange(n).reshape(g, g)
+    rows, cols, vals = [], [], []
+    diag = np.zeros((g, g))
+
+    def face(a1, a2):
+        return 2.0 / (1.0 / a1 + 1.0 / a2)
+
+    # x faces
+    fx = face(a[:, :-1], a[:, 1:])
+    rows += [idx[:, :-1].ravel(), idx[:, 1:].ravel()]
+    cols += [idx[:, 1:].ravel(), idx[:, :-1].ravel()]
+    vals += [-fx.ravel(), -fx.ravel()]
+    diag[:, :-1] += fx
+    diag[:, 1:] += fx
+    diag[:, 0] += 2 * a[:, 0]
+    diag[:, -1] += 2 * a[:, -1]
+    # y faces (scaled by eps)
+    fy = eps * face(a[:-1, :], a[1:, :])
+    rows += [idx[:-1, :].ravel(), idx[1:, :].ravel()]
+    cols += [idx[1:, :].ravel(), idx[:-1, :].ravel()]
+    vals += [-fy.ravel(), -fy.ravel()]
+    diag[:-1, :] += fy
+    diag[1:, :] += fy
+    diag[0, :] += 2 * eps * a[0, :]
+    diag[-1, :] += 2 * eps * a[-1, :]
+    rows.append(idx.ravel())
+    cols.append(idx.ravel())
+    vals.append(diag.ravel())
+    m = sp.coo_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                      shape=(n, n))
+    return from_scipy(m)
+
+
+def random_spd(n: int, nnz_per_row: int = 8, rng: np.random.Generator | None = None) -> CSR:
+    rng = np.random.default_rng(0) if rng is None else rng
+    k = max(1, (nnz_per_row - 1) // 2)
+    r = np.repeat(np.arange(n), k)
+    c = rng.integers(0, n, size=r.size)
+    keep = r != c
+    r, c = r[keep], c[keep]
+    v = rng.standard_normal(r.size)
+    m = sp.coo_matrix((np.concatenate([v, v]), (np.concatenate([r, c]), np.concatenate([c, r]))),
+                      shape=(n, n)).tocsr()
+    m.sum_duplicates()
+    rowsum = np.asarray(abs(m).sum(axis=1)).ravel()
+    m = m + sp.diags(rowsum + 1.0)
+    return from_scipy(m)
+
+
+def random_lower(n: int, density: float, rng: np.random.Generator | None = None,
+                 unit_scale: bool = False) -> CSR:
+    """Random lower-triangular CSR, diagonal last in every row."""
+    rng = np.random.default_rng(0) if rng is None else rng
+    m = sp.random(n, n, density=density, format="coo", random_state=rng,
+                  data_rvs=lambda s: rng.uniform(-1.0, 1.0, s))
+    low = m.row > m.col
+    r, c, v = m.row[low], m.col[low], m.data[low]
+    if unit_scale:
+        v = np.ones_like(v)
+    d = np.full(n, 2.0 if not unit_scale else 1.0) + (0 if unit_scale else rng.uniform(0, 1, n))
+    mm = sp.coo_matrix((np.concatenate([v, d]), (np.concatenate([r, np.arange(n)]),
+                                                  np.concatenate([c, np.arange(n)]))), shape=(n, n))
+    return from_scipy(mm)
+
+
+# ---- triangle extraction / transposition ---------------------------------
+
+def tril(a: CSR, k: int = 0) -> CSR:
+    return from_scipy(sp.tril(a.scipy(), k=k))
+
+
+def triu(a: CSR, k: int = 0) -> CSR:
+    return from_scipy(sp.triu(a.scipy(), k=k))
+
+
+def transpose(a: CSR) -> CSR:
+    """CSR of A^T (equivalently: the CSC arrays of A)."""
+    return from_scipy(a.scipy().T.tocsr())
+
+
+def diag_ptr(a: CSR) -> np.ndarray:
+    """Index of the diagonal entry of each row (the ILU0 ``A_diag``/``ua``)."""
+    out = np.empty(a.n, dtype=np.int32)
+    for_rows = np.repeat(np.arange(a.n), np.diff(a.p))
+    hit = np.nonzero(a.i == for_rows)[0]
+    out[for_rows[hit]] = hit
+    return out
+
+
+def levels_wavefront(a: CSR) -> int:
+    """Number of wavefront levels of tril(a) (for sizing only)."""
+    L = tril(a)
+    lev = np.zeros(a.n, dtype=np.int64)
+    p, i = L.p, L.i
+    for r in range(a.n):
+        m = -1
+        for j in range(p[r], p[r + 1] - 1):
+            m = max(m, lev[i[j]])
+        lev[r] = m + 1
+    return int(lev.max() + 1) if a.n else 0

@@ -1,0 +1,300 @@
+"""Device-resident plans over the C ABI, with torch tensors as device memory.
+
+``TriPlan`` (a level-packed triangle), ``CsrPlan`` (SpMV), the GPU
+factorisations, the Krylov drivers, the adjoint and ``BatchPlan``.  Calls
+are stream-ordered on torch's current CUDA stream unless a stream is given,
+so they interleave correctly with torch work on the same stream.  PyTorch
+only provides the device memory and the stream here; all compute is in
+``libgbsym.so``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import KrylovResult, TriInfo, check, lib
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _stream(stream):
+    if stream is not None:
+        return C.c_void_p(int(stream))
+    torch = _torch()
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dev_ptr(t, dtype=None, name="tensor"):
+    torch = _torch()
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise TypeError("%s must be a CUDA tensor" % name)
+    if dtype is not None and t.dtype != dtype:
+        raise TypeError("%s must be %s, got %s" % (name, dtype, t.dtype))
+    if not t.is_contiguous():
+        raise TypeError("%s must be contiguous" % name)
+    return C.c_void_p(t.data_ptr())
+
+
+def _host_or_dev(a, np_dtype, torch_dtype, name):
+    """(pointer, on_device, keepalive) for a numpy array or CUDA tensor."""
+    if a is None:
+        return None, None, None
+    torch = _torch()
+    if isinstance(a, torch.Tensor):
+        return _dev_ptr(a, torch_dtype, name), True, a
+    arr = np.ascontiguousarray(a, dtype=np_dtype)
+    return arr.ctypes.data_as(C.c_void_p), False, arr
+
+
+def _dtype_code(dtype):
+    if dtype in ("f64", "float64", np.float64, L.F64):
+        return L.F64
+    if dtype in ("f32", "float32", np.float32, L.F32):
+        return L.F32
+    torch = _torch()
+    if dtype == torch.float64:
+        return L.F64
+    if dtype == torch.float32:
+        return L.F32
+    raise ValueError("unsupported dtype %r" % (dtype,))
+
+
+class TriPlan:
+    """A triangle packed for the GPU executor (see gbsym_tri_create)."""
+
+    def __init__(self, n, p, i, x, kind=L.LOWER_DIAG_LAST, diags=None, dtype="f64",
+                 level_ptr=None, level_set=None, stream=None):
+        torch = _torch()
+        pp, dev_p, kp = _host_or_dev(p, np.int32, torch.int32, "p")
+        ii, dev_i, ki = _host_or_dev(i, np.int32, torch.int32, "i")
+        xx, dev_x, kx = _host_or_dev(x, np.float64, torch.float64, "x")
+        dd, dev_d, kd = _host_or_dev(diags, np.int32, torch.int32, "diags")
+        on_dev = bool(dev_p)
+        if len({v for v in (dev_p, dev_i, dev_x, dev_d) if v is not None}) > 1:
+            raise TypeError("p, i, x, diags must all be host arrays or all CUDA tensors")
+        lpp = lsp = None
+        levels = 0
+        if level_set is not None:
+            if on_dev:
+                lpp, _, klp = _host_or_dev(level_ptr, np.int32, torch.int32, "level_ptr")
+                lsp, _, kls = _host_or_dev(level_set, np.int32, torch.int32, "level_set")
+            else:
+                klp = np.ascontiguousarray(level_ptr, dtype=np.int32)
+                kls = np.ascontiguousarray(level_set, dtype=np.int32)
+                lpp, lsp = klp.ctypes.data_as(C.c_void_p), kls.ctypes.data_as(C.c_void_p)
+            levels = int(len(level_ptr) - 1)
+        h = C.c_void_p()
+        check(lib().gbsym_tri_create(C.byref(h), int(n), pp, ii, xx, dd, int(kind), _dtype_code(dtype),
+                                     1 if on_dev else 0, lpp, lsp, levels, _stream(stream)),
+              "gbsym_tri_create")
+        self._h = h
+        self.n = int(n)
+        self.kind = kind
+        self.dtype = _dtype_code(dtype)
+        del kp, ki, kx, kd
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> TriInfo:
+        inf = TriInfo()
+        check(lib().gbsym_tri_get_info(self._h, C.byref(inf)), "gbsym_tri_get_info")
+        return inf
+
+    def schedule(self):
+        inf = self.info()
+        lp = np.zeros(inf.levels + 1, dtype=np.int32)
+        ls = np.zeros(max(self.n, 1), dtype=np.int32)
+        check(lib().gbsym_tri_get_schedule(self._h, lp.ctypes.data_as(C.c_void_p),
+                                           ls.ctypes.data_as(C.c_void_p)), "gbsym_tri_get_schedule")
+        return inf.levels, lp, ls[: self.n]
+
+    def set_exec(self, exec_mode: int):
+        check(lib().gbsym_tri_set_exec(self._h, int(exec_mode)), "gbsym_tri_set_exec")
+
+    def solve(self, x, layout=L.ROW_MAJOR, stream=None):
+        """In place on a CUDA tensor of shape (n,) or (n, k) row-major
+        (or (k, n) with layout=COL_MAJOR, i.e. column-major n x k)."""
+        torch = _torch()
+        if x.dim() == 1:
+            k = 1
+        elif layout == L.ROW_MAJOR:
+            k = x.shape[1]
+        else:
+            k = x.shape[0]
+        dt = _dtype_code(x.dtype)
+        check(lib().gbsym_tri_solve(self._h, _dev_ptr(x, None, "x"), int(k), int(layout), dt,
+                                    _stream(stream)), "gbsym_tri_solve")
+        del torch
+        return x
+
+    def solve_b(self, b, x, stream=None):
+        torch = _torch()
+        check(lib().gbsym_tri_solve_b(self._h, _dev_ptr(b, torch.float64, "b"),
+                                      _dev_ptr(x, torch.float64, "x"), _stream(stream)),
+              "gbsym_tri_solve_b")
+        return x
+
+    def solve_host(self, x: np.ndarray, layout=L.COL_MAJOR):
+        """End to end on host memory (numpy float64, pinned or pageable)."""
+        if x.dtype != np.float64 or not x.flags.c_contiguous:
+            raise TypeError("x must be a C-contiguous float64 array")
+        k = 1 if x.ndim == 1 else (x.shape[0] if layout == L.COL_MAJOR else x.shape[1])
+        check(lib().gbsym_tri_solve_host(self._h, x.ctypes.data_as(C.c_void_p), int(k), int(layout)),
+              "gbsym_tri_solve_host")
+        return x
+
+    def solve_host_ptr(self, ptr: int, k: int, layout=L.ROW_MAJOR):
+        check(lib().gbsym_tri_solve_host(self._h, C.c_void_p(ptr), int(k), int(layout)),
+              "gbsym_tri_solve_host")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gbsym_tri_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class CsrPlan:
+    """A CSR matrix resident on the GPU for SpMV."""
+
+    def __init__(self, n, p, i, x, ncols=None, dtype="f64", stream=None):
+        torch = _torch()
+        pp, dev, kp = _host_or_dev(p, np.int32, torch.int32, "p")
+        ii, _, ki = _host_or_dev(i, np.int32, torch.int32, "i")
+        xx, _, kx = _host_or_dev(x, np.float64, torch.float64, "x")
+        h = C.c_void_p()
+        check(lib().gbsym_csr_create(C.byref(h), int(n), int(n if ncols is None else ncols), pp, ii, xx,
+                                     _dtype_code(dtype), 1 if dev else 0, _stream(stream)),
+              "gbsym_csr_create")
+        self._h = h
+        self.n = int(n)
+        del kp, ki, kx
+
+    @property
+    def handle(self):
+        return self._h
+
+    def spmv(self, x, y, stream=None):
+        check(lib().gbsym_csr_spmv(self._h, _dev_ptr(x, None, "x"), _dev_ptr(y, None, "y"),
+                                   _dtype_code(x.dtype), _stream(stream)), "gbsym_csr_spmv")
+        return y
+
+    def spmv_axpby(self, x, y, z, alpha, beta, stream=None):
+        check(lib().gbsym_csr_spmv_axpby(self._h, _dev_ptr(x), _dev_ptr(y), _dev_ptr(z), float(alpha),
+                                         float(beta), _stream(stream)), "gbsym_csr_spmv_axpby")
+        return z
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gbsym_csr_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def ilu0_device(n, Ap, Ai, Ax, A_diag, l, stream=None):
+    torch = _torch()
+    check(lib().gbsym_ilu0_device(int(n), _dev_ptr(Ap, torch.int32), _dev_ptr(Ai, torch.int32),
+                                  _dev_ptr(Ax, torch.float64), _dev_ptr(A_diag, torch.int32),
+                                  _dev_ptr(l, torch.float64), _stream(stream)), "gbsym_ilu0_device")
+    return l
+
+
+def ic0_device(n, val, rowPtr, rowIdx, stream=None):  # noqa: N803
+    torch = _torch()
+    check(lib().gbsym_ic0_device(int(n), _dev_ptr(val, torch.float64), _dev_ptr(rowPtr, torch.int32),
+                                 _dev_ptr(rowIdx, torch.int32), _stream(stream)), "gbsym_ic0_device")
+    return val
+
+
+def pcg(A: CsrPlan, Lf: TriPlan, Lt: TriPlan, b, x, tol=1e-10, maxit=10000, stream=None):
+    res = KrylovResult()
+    st = lib().gbsym_pcg(A.handle, Lf.handle, Lt.handle, _dev_ptr(b), _dev_ptr(x), float(tol), int(maxit),
+                         C.byref(res), _stream(stream))
+    check(st, "gbsym_pcg")
+    return res
+
+
+def gmres(A: CsrPlan, Lu: TriPlan, U: TriPlan, b, x, mr=30, maxit=1000, tol=1e-10, stream=None):
+    res = KrylovResult()
+    st = lib().gbsym_gmres(A.handle, Lu.handle, U.handle, _dev_ptr(b), _dev_ptr(x), int(mr), int(maxit),
+                           float(tol), C.byref(res), _stream(stream))
+    check(st, "gbsym_gmres")
+    return res
+
+
+def tri_adjoint(Lt: TriPlan, n, Lp, Li, X, g, grad, stream=None):
+    """g <- L^{-T} g (in place) and grad[p] = -sum_r g[row p, r] X[col p, r]."""
+    torch = _torch()
+    k = 1 if X.dim() == 1 else X.shape[1]
+    check(lib().gbsym_tri_adjoint(Lt.handle, int(n), _dev_ptr(Lp, torch.int32), _dev_ptr(Li, torch.int32),
+                                  _dev_ptr(X, torch.float64), _dev_ptr(g, torch.float64), int(k),
+                                  _dev_ptr(grad, torch.float64), _stream(stream)), "gbsym_tri_adjoint")
+    return g, grad
+
+
+class BatchPlan:
+    """Many lower-triangular CSR systems (diagonal last) solved together."""
+
+    def __init__(self, systems, dtype="f64", stream=None):
+        nsys = len(systems)
+        self._keep = []
+        ns = (C.c_int * nsys)()
+        ps = (C.c_void_p * nsys)()
+        is_ = (C.c_void_p * nsys)()
+        xs = (C.c_void_p * nsys)()
+        for q, (n, p, i, x) in enumerate(systems):
+            p = np.ascontiguousarray(p, dtype=np.int32)
+            i = np.ascontiguousarray(i, dtype=np.int32)
+            x = np.ascontiguousarray(x, dtype=np.float64)
+            self._keep += [p, i, x]
+            ns[q] = int(n)
+            ps[q] = p.ctypes.data
+            is_[q] = i.ctypes.data
+            xs[q] = x.ctypes.data
+        h = C.c_void_p()
+        check(lib().gbsym_batch_create(C.byref(h), nsys, ns, ps, is_, xs, _dtype_code(dtype),
+                                       _stream(stream)), "gbsym_batch_create")
+        self._h = h
+        self._keep = None
+        self.nsys = nsys
+        off = np.zeros(nsys + 1, dtype=np.int64)
+        check(lib().gbsym_batch_row_offsets(h, off.ctypes.data_as(C.c_void_p)), "gbsym_batch_row_offsets")
+        self.offsets = off
+
+    def solve(self, x, stream=None):
+        k = 1 if x.dim() == 1 else x.shape[1]
+        check(lib().gbsym_batch_solve(self._h, _dev_ptr(x), int(k), _dtype_code(x.dtype), _stream(stream)),
+              "gbsym_batch_solve")
+        return x
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gbsym_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def kernel_launches() -> int:
+    return int(lib().gbsym_kernel_launches())

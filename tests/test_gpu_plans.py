@@ -1,0 +1,159 @@
+"""Device-resident plans at the workload sizes: multi-RHS, FP32, executors,
+layouts, end-to-end host solves -- against the oracle."""
+import numpy as np
+import pytest
+import torch
+
+from sympiler_gb300 import matgen as mg
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def c2_factor(orc):
+    """IC0 factor of the 3D 7-point Laplacian 64^3 + 1e-2 I."""
+    A = mg.lap3d(64, 1e-2)
+    U = mg.triu(A)
+    f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+    assert ok
+    Lt = mg.CSR(U.n, U.p, U.i, f)  # CSC of L = upper CSR of L^T
+    L = mg.transpose(Lt)
+    return A, L, Lt
+
+
+def _oracle_mrhs(orc, L, B_rowmajor):
+    n, k = B_rowmajor.shape
+    X = np.ascontiguousarray(B_rowmajor.T.copy())  # column-major n x k
+    orc.sptrsv_csr_mrhs(n, *L.astuple(), X, k, 8)
+    return X.T
+
+
+@pytest.mark.parametrize("k", [1, 3, 8, 64])
+def test_c2_forward_multi_rhs_bit_exact(gpu, orc, c2_factor, k):
+    from sympiler_gb300.plans import TriPlan
+    _, L, _ = c2_factor
+    rng = np.random.default_rng(k)
+    B = rng.standard_normal((L.n, k))
+    ref = _oracle_mrhs(orc, L, B)
+    plan = TriPlan(L.n, *L.astuple())
+    assert plan.info().levels == 190
+    x = torch.from_numpy(B.copy()).cuda()
+    plan.solve(x if k > 1 else x.view(-1))
+    torch.cuda.synchronize()
+    assert np.array_equal(x.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("exec_mode", [1, 3])
+def test_executors_agree(gpu, orc, c2_factor, exec_mode):
+    from sympiler_gb300.plans import TriPlan
+    _, L, Lt = c2_factor
+    rng = np.random.default_rng(7)
+    b = rng.standard_normal(L.n)
+    ref = b.copy()
+    orc.sptrsv_csr(L.n, *L.astuple(), ref)
+    plan = TriPlan(L.n, *L.astuple())
+    plan.set_exec(exec_mode)
+    x = torch.from_numpy(b.copy()).cuda()
+    plan.solve(x)
+    torch.cuda.synchronize()
+    assert np.array_equal(x.cpu().numpy(), ref)
+    # the transposed (backward) solve on the CSC of L
+    ref_t = b.copy()
+    orc.ltsolve(L.n, *Lt.astuple(), ref_t)
+    from sympiler_gb300._lib import UPPER_DIAG_FIRST
+    pt = TriPlan(L.n, *Lt.astuple(), kind=UPPER_DIAG_FIRST)
+    pt.set_exec(exec_mode)
+    x = torch.from_numpy(b.copy()).cuda()
+    pt.solve(x)
+    torch.cuda.synchronize()
+    assert np.array_equal(x.cpu().numpy(), ref_t)
+
+
+def test_fp32_storage_bit_exact_vs_fp32_oracle(gpu, orc, c2_factor):
+    from sympiler_gb300.plans import TriPlan
+    _, L, _ = c2_factor
+    rng = np.random.default_rng(3)
+    b = rng.standard_normal(L.n).astype(np.float32)
+    ref = b.copy()
+    orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), ref)
+    plan = TriPlan(L.n, *L.astuple(), dtype="f32")
+    x = torch.from_numpy(b.copy()).cuda()
+    plan.solve(x)
+    torch.cuda.synchronize()
+    assert np.array_equal(x.cpu().numpy(), ref)
+    B = rng.standard_normal((L.n, 16)).astype(np.float32)
+    xb = torch.from_numpy(B.copy()).cuda()
+    plan.solve(xb)
+    torch.cuda.synchronize()
+    got = xb.cpu().numpy()
+    for c in (0, 7, 15):
+        r = np.ascontiguousarray(B[:, c])
+        orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), r)
+        assert np.array_equal(got[:, c], r)
+
+
+def test_column_major_and_host_solve(gpu, orc, c2_factor):
+    from sympiler_gb300._lib import COL_MAJOR
+    from sympiler_gb300.plans import TriPlan
+    _, L, _ = c2_factor
+    rng = np.random.default_rng(9)
+    k = 5
+    Bc = rng.standard_normal((k, L.n))  # column-major n x k == k rows of n
+    ref = Bc.copy()
+    orc.sptrsv_csr_mrhs(L.n, *L.astuple(), ref, k, 8)
+    plan = TriPlan(L.n, *L.astuple())
+    x = torch.from_numpy(Bc.copy()).cuda()
+    plan.solve(x, layout=COL_MAJOR)
+    torch.cuda.synchronize()
+    assert np.array_equal(x.cpu().numpy(), ref)
+    h = Bc.copy()
+    plan.solve_host(h, layout=COL_MAJOR)
+    assert np.array_equal(h, ref)
+
+
+def test_plan_from_device_arrays_and_schedule(gpu, orc):
+    from sympiler_gb300.plans import TriPlan
+    A = mg.lap2d(100)
+    L = mg.tril(A)
+    nl, lp, ls = orc.build_levelset_csr(L.n, L.p, L.i)
+    dev = [torch.from_numpy(a.copy()).cuda() for a in L.astuple()]
+    plan = TriPlan(L.n, *dev, level_ptr=torch.from_numpy(lp).cuda(), level_set=torch.from_numpy(ls).cuda())
+    got = plan.schedule()
+    assert got[0] == nl and np.array_equal(got[1], lp) and np.array_equal(got[2], ls)
+    b = np.random.default_rng(1).uniform(-1, 1, L.n)
+    ref = b.copy()
+    orc.sptrsv_csr(L.n, *L.astuple(), ref)
+    x = torch.from_numpy(b.copy()).cuda()
+    plan.solve(x)
+    torch.cuda.synchronize()
+    assert np.array_equal(x.cpu().numpy(), ref)
+
+
+def test_batch_uneven_systems(gpu, orc):
+    from sympiler_gb300.plans import BatchPlan
+    rng = np.random.default_rng(4)
+    systems, Ls = [], []
+    for q in range(24):
+        if q % 5 == 4:
+            A = mg.random_spd(int(rng.integers(300, 3000)), 8, rng)
+        else:
+            A = mg.lap2d(int(rng.integers(30, 80)), int(rng.integers(30, 80)))
+            A = mg.from_scipy(A.scipy() + float(rng.uniform(1e-3, 1)) * __import__("scipy").sparse.eye(A.n))
+        U = mg.triu(A)
+        f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+        assert ok
+        L = mg.transpose(mg.CSR(U.n, U.p, U.i, f))
+        Ls.append(L)
+        systems.append((L.n, *L.astuple()))
+    bp = BatchPlan(systems)
+    k = 8
+    N = int(bp.offsets[-1])
+    B = rng.standard_normal((N, k))
+    x = torch.from_numpy(B.copy()).cuda()
+    bp.solve(x)
+    torch.cuda.synchronize()
+    got = x.cpu().numpy()
+    for q, L in enumerate(Ls):
+        a, z = bp.offsets[q], bp.offsets[q + 1]
+        ref = _oracle_mrhs(orc, L, B[a:z])
+        assert np.array_equal(got[a:z], ref), q

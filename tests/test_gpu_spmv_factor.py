@@ -1,0 +1,108 @@
+"""GPU SpMV and incomplete factorisations against the reference's known
+answers and the oracle (bit-exact: same operation order, no contraction)."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+from sympiler_gb300 import matgen as mg
+
+pytestmark = pytest.mark.gpu
+
+
+def test_spmv_catch_known_answers(gpu):
+    from sympiler_gb300 import sym_lib
+    for name in ("catch_spmv_4x4", "catch_spmv_10x10"):
+        d = golden(name)
+        n = len(d["Ap"]) - 1
+        y = np.zeros(n)
+        sym_lib.spmv_csr(n, d["Ap"], d["Ai"], d["Ax"], d["x"], y)
+        assert np.array_equal(y, d["z"])
+        y = np.zeros(n)
+        sym_lib.spmv_csr_parallel(n, d["Ap"], d["Ai"], d["Ax"], d["x"], y)
+        assert np.array_equal(y, d["z"])
+
+
+def test_spmv_c1_fixture(gpu):
+    from sympiler_gb300 import sym_lib
+    d = golden("c1_lap2d_100")
+    n = len(d["Ap"]) - 1
+    y = np.zeros(n)
+    sym_lib.spmv_csr(n, d["Ap"], d["Ai"], d["Ax"], d["v"], y)
+    assert np.array_equal(y, d["y"])
+    z = d["z0"].copy()
+    sym_lib.spmv_csr(n, d["Ap"], d["Ai"], d["Ax"], d["v"], d["b"], z, float(d["a"]), float(d["bb"]))
+    assert np.array_equal(z, d["z"])
+
+
+@pytest.mark.parametrize("gen", ["lap3d64", "convdiff48", "random"])
+def test_spmv_plan_large_fp64_fp32(gpu, orc, gen):
+    from sympiler_gb300.plans import CsrPlan
+    rng = np.random.default_rng(2)
+    if gen == "lap3d64":
+        A = mg.lap3d(64, 1e-2)
+    elif gen == "convdiff48":
+        A = mg.convdiff3d(48)
+    else:
+        A = mg.random_spd(50000, 40, rng)  # rows up to ~80 entries
+    v = rng.uniform(-1, 1, A.n)
+    ref = np.zeros(A.n)
+    orc.spmv_csr(A.n, *A.astuple(), v, ref)
+    P = CsrPlan(A.n, *A.astuple())
+    y = torch.zeros(A.n, dtype=torch.float64, device="cuda")
+    P.spmv(torch.from_numpy(v).cuda(), y)
+    torch.cuda.synchronize()
+    assert np.array_equal(y.cpu().numpy(), ref)
+    P32 = CsrPlan(A.n, *A.astuple(), dtype="f32")
+    v32 = v.astype(np.float32)
+    ref32 = np.zeros(A.n, dtype=np.float32)
+    orc.spmv_csr_f32(A.n, A.p, A.i, A.x.astype(np.float32), v32, ref32)
+    y32 = torch.zeros(A.n, dtype=torch.float32, device="cuda")
+    P32.spmv(torch.from_numpy(v32).cuda(), y32)
+    torch.cuda.synchronize()
+    assert np.array_equal(y32.cpu().numpy(), ref32)
+
+
+def test_ilu0_and_ic0_fixtures(gpu):
+    from sympiler_gb300 import sym_lib
+    d = golden("ilu0_convdiff_8")
+    n = len(d["Ap"]) - 1
+    l = np.zeros_like(d["Ax"])
+    sym_lib.spilu0_csr(n, int(d["Ap"][n]), d["Ap"], d["Ai"], d["Ax"], d["diag"], l)
+    assert np.array_equal(l, d["lu"])
+    for name in ("ic0_lap3d_10", "ic0_random_spd_2000"):
+        g = golden(name)
+        n = len(g["Up"]) - 1
+        v = g["Ux"].copy()
+        sym_lib.spic0_csr(n, v, g["Up"], g["Ui"])
+        assert np.array_equal(v, g["factor"]), name
+
+
+def test_factors_at_workload_size(gpu, orc):
+    from sympiler_gb300.plans import ic0_device, ilu0_device
+    A = mg.lap3d(64, 1e-2)
+    U = mg.triu(A)
+    ref, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+    v = torch.from_numpy(U.x.copy()).cuda()
+    ic0_device(U.n, v, torch.from_numpy(U.p).cuda(), torch.from_numpy(U.i).cuda())
+    torch.cuda.synchronize()
+    assert np.array_equal(v.cpu().numpy(), ref)
+    C = mg.convdiff3d(40)
+    d = mg.diag_ptr(C)
+    refl, ok = orc.spilu0_csr(C.n, C.p, C.i, C.x, d)
+    out = torch.zeros(C.nnz, dtype=torch.float64, device="cuda")
+    ilu0_device(C.n, *(torch.from_numpy(a).cuda() for a in (C.p, C.i, C.x, d)), out)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), refl)
+
+
+def test_ic0_pivot_error(gpu):
+    from sympiler_gb300 import sym_lib
+    from sympiler_gb300._lib import ERR_PIVOT, GbsymError
+    A = mg.lap2d(8)
+    A = mg.from_scipy(A.scipy() - 8.0 * __import__("scipy").sparse.eye(A.n))  # indefinite
+    U = mg.triu(A)
+    v = U.x.copy()
+    with pytest.raises(GbsymError) as e:
+        sym_lib.spic0_csr(U.n, v, U.p, U.i)
+    assert e.value.status == ERR_PIVOT
