@@ -10,11 +10,12 @@
 //
 // IC0 restates spic0_csr (sparse_blas/spic0.cpp:106-128), which is
 // right-looking on the upper CSR of A.  The same values come out of a
-// left-looking sweep: entry (c, q) receives -= L_ic * L_iq from every
-// earlier row i holding both c and q, in ascending i, then the diagonal
-// takes its square root and the off-diagonals are divided by it.  The rows
-// i feeding row c are the column c of the upper pattern, found through its
-// transpose; rows run one warp each, one launch per wavefront level.
+// left-looking sweep: row c receives its updates from the earlier rows i
+// that hold column c, in ascending i (see k_ic0_rows for which entry each
+// such row updates), then the diagonal takes its square root and the
+// off-diagonals are divided by it.  The rows i feeding row c are the column
+// c of the upper pattern, found through its transpose; rows run one warp
+// each, one launch per wavefront level.
 #include <cub/cub.cuh>
 
 #include <algorithm>
@@ -182,8 +183,15 @@ void transpose_pattern(int n, int nnz, const int *p, const int *ci, Transposed &
   check_launch();
 }
 
-// Row c of the upper factor: updates from the rows i listed in the
-// transposed pattern (ascending), then square root and scaling.
+// Row c of the upper factor.  The reference's inner scan
+// (spic0.cpp:117-123: `for (l = m; l < Lp[i+1] && Li[l+1] <= Li[k]; l++)
+// if (Li[l] == Li[k]) ...`) tests the NEXT column before the match, so
+// within row i it reaches a matching position only when that position is
+// the last entry of row i (the following read is the next row's diagonal,
+// i+1 <= Li[k]).  Row i therefore updates exactly one entry of row c: the
+// one in the column of row i's last entry, if row c holds it.  Lanes find
+// those targets and form the products for up to 32 rows i at a time; lane
+// 0 applies the subtractions in ascending i, the reference's order.
 __global__ void k_ic0_rows(const int *__restrict__ up, const int *__restrict__ ui, double *val,
                            const int *__restrict__ lp, const int *__restrict__ li,
                            const int *__restrict__ lsrc, const int *__restrict__ order, int r0,
@@ -194,15 +202,25 @@ __global__ void k_ic0_rows(const int *__restrict__ up, const int *__restrict__ u
   const int c = order[kk];
   const int a = up[c], z = up[c + 1];
   // transposed row c: rows i <= c holding column c; the last one is c itself
-  for (int t = lp[c]; t < lp[c + 1] - 1; ++t) {
-    const int i = li[t];
-    const int m = lsrc[t];
-    const double lic = val[m];
-    const int ie = up[i + 1];
-    for (int k = a + lane; k < z; k += 32) {
-      const int l = find_col(ui, m, ie, ui[k]);
-      if (l >= 0) val[k] = sub_rn(val[k], mul_rn(lic, val[l]));
+  const int t_end = lp[c + 1] - 1;
+  for (int t0 = lp[c]; t0 < t_end; t0 += 32) {
+    const int t = t0 + lane;
+    int kpos = -1;
+    double prod = 0.0;
+    if (t < t_end) {
+      const int i = li[t];
+      const int m = lsrc[t];
+      const int last = up[i + 1] - 1;
+      kpos = find_col(ui, a, z, ui[last]);
+      if (kpos >= 0) prod = mul_rn(val[m], val[last]);
     }
+    const int cnt = min(32, t_end - t0);
+    for (int q = 0; q < cnt; ++q) {
+      const int kp = __shfl_sync(0xffffffffu, kpos, q);
+      const double pr = __shfl_sync(0xffffffffu, prod, q);
+      if (lane == 0 && kp >= 0) val[kp] = sub_rn(val[kp], pr);
+    }
+    __syncwarp();
   }
   double d = 0.0;
   if (lane == 0) {
