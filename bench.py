@@ -250,6 +250,8 @@ def main():
     Lt = mg.CSR(U.n, U.p, U.i, vals.cpu().numpy())
     L = mg.transpose(Lt)
     plan = TriPlan(L.n, *L.astuple())
+    from sympiler_gb300._lib import EXEC_NAMES
+    tuned = {"k1": EXEC_NAMES.get(plan.autotune(k=1)), "k%d" % k: EXEC_NAMES.get(plan.autotune(k=k))}
     info = plan.info()
     n = L.n
     byt = algorithmic_bytes(L.nnz, n, k)
@@ -337,8 +339,8 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(config(g, k), levels=info.levels, nnz_L=int(L.nnz),
-                           executor={1: "levelset-graph", 2: "syncfree", 3: "oneblock"}.get(info.exec),
+            "config": dict(config(g, k), levels=info.levels, nnz_L=int(L.nnz), executor=tuned,
+                           arithmetic="exact (reference operation order, bit-identical)",
                            wall_s_timed_region=wall),
             "roofline": {"bound": "hbm", "achieved": byt / t_step / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": byt / t_step / 1e9 / peak, "peak_source": peak_src,
@@ -377,6 +379,40 @@ def main():
         b1 = algorithmic_bytes(L.nnz, n, 1)
         extras["sptrsv_1rhs"] = {"us": t1 * 1e6, "gbs": b1 / t1 / 1e9, "levels": info.levels,
                                  "us_per_level": t1 * 1e6 / info.levels}
+
+        # every executor on the same factor, 1 and k right-hand sides
+        def time_exec(mode, xbuf, src, reps=5):
+            plan.set_exec(mode)
+            for _ in range(2):
+                xbuf.copy_(src)
+                plan.solve(xbuf)
+            tt = []
+            for _ in range(reps):
+                xbuf.copy_(src)
+                flush.fill_(5)
+                a0 = torch.cuda.Event(enable_timing=True)
+                a1 = torch.cuda.Event(enable_timing=True)
+                a0.record(stream)
+                plan.solve(xbuf)
+                a1.record(stream)
+                torch.cuda.synchronize()
+                tt.append(a0.elapsed_time(a1) * 1e3)
+            plan.check()
+            return statistics.median(tt)
+        ex = {}
+        for arith_name, arith in (("exact", 0), ("fused", 1)):
+            plan.set_arith(arith)
+            for name, mode in (("levelset_graph_pdl", 1), ("syncfree", 2), ("persistent", 4), ("oneblock", 3),
+                               ("cluster", 5)):
+                key = "%s_%s" % (name, arith_name)
+                ex[key] = {"us_1rhs": time_exec(mode, x1w, x1)}
+                if mode != 3:
+                    ex[key]["us_%drhs" % k] = time_exec(mode, X, B)
+        plan.set_arith(0)
+        plan.set_exec(0)
+        ex["autotuned"] = {"k1": EXEC_NAMES.get(plan.autotune(k=1)),
+                           "k%d" % k: EXEC_NAMES.get(plan.autotune(k=k))}
+        extras["executors"] = ex
         # IC0-PCG to 1e-10 on C2 (FP64 throughout)
         Pt = TriPlan(n, *Lt.astuple(), kind=UPPER_DIAG_FIRST)
         Ac = CsrPlan(n, *A.astuple())

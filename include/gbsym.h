@@ -175,8 +175,19 @@ enum gbsym_exec {
   GBSYM_EXEC_AUTO = 0,      /* autotuner choice                            */
   GBSYM_EXEC_LEVELSET = 1,  /* one launch per level, captured in a graph   */
   GBSYM_EXEC_SYNCFREE = 2,  /* one persistent launch, per-row ready flags  */
-  GBSYM_EXEC_ONEBLOCK = 3   /* one thread block sweeps all levels          */
+  GBSYM_EXEC_ONEBLOCK = 3,  /* one thread block sweeps all levels          */
+  GBSYM_EXEC_PERSISTENT = 4, /* one cooperative launch, grid barrier/level */
+  GBSYM_EXEC_CLUSTER = 5     /* thread-block clusters, hardware cluster
+                                barrier per level; k > 1 splits columns
+                                over clusters                             */
 };
+
+/* Arithmetic of the row updates.  EXACT: every x_i -= L_ij x_j is a
+ * rounded product followed by a rounded difference and the division is
+ * correctly rounded -- the reference's operation sequence, bit-identical
+ * results.  FUSED: one fused multiply-add per entry (results within a few
+ * ulps of the reference; fewer FP64 operations). */
+enum gbsym_arith { GBSYM_ARITH_EXACT = 0, GBSYM_ARITH_FUSED = 1 };
 
 typedef struct gbsym_tri_s *gbsym_tri;
 
@@ -205,6 +216,19 @@ int gbsym_tri_destroy(gbsym_tri t);
 int gbsym_tri_get_info(gbsym_tri t, gbsym_tri_info *info);
 /* Force an executor (GBSYM_EXEC_*); AUTO restores the autotuned choice. */
 int gbsym_tri_set_exec(gbsym_tri t, int exec);
+/* Choose the row arithmetic (GBSYM_ARITH_*); EXACT is the default. */
+int gbsym_tri_set_arith(gbsym_tri t, int arith);
+/* Times every executor on this plan for k right-hand sides of the given
+ * dtype (on scratch memory; the caller's data is not touched), keeps the
+ * fastest for later solves with k (k == 1 or k > 1) and remembers it for
+ * plans with the same level count, mean row length, k and dtype.  The
+ * chosen GBSYM_EXEC_* is returned in *chosen when non-NULL.  Synchronises
+ * the stream. */
+int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, int *chosen);
+/* Waits for `stream` and returns the first error a device-side check of
+ * this plan recorded since the last call (e.g. GBSYM_ERR_TIMEOUT from a
+ * bounded wait), clearing it; GBSYM_OK when none. */
+int gbsym_tri_check(gbsym_tri t, void *stream);
 /* Copy the schedule into host buffers of levels+1 and n ints. */
 int gbsym_tri_get_schedule(gbsym_tri t, int *level_ptr, int *level_set);
 

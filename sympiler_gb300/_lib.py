@@ -63,6 +63,9 @@ SIGNATURES = {
     "gbsym_tri_destroy": (_int, [_vp]),
     "gbsym_tri_get_info": (_int, [_vp, C.POINTER(TriInfo)]),
     "gbsym_tri_set_exec": (_int, [_vp, _int]),
+    "gbsym_tri_check": (_int, [_vp, _vp]),
+    "gbsym_tri_set_arith": (_int, [_vp, _int]),
+    "gbsym_tri_autotune": (_int, [_vp, _int, _int, _vp, _pi]),
     "gbsym_tri_get_schedule": (_int, [_vp, _vp, _vp]),
     "gbsym_tri_solve": (_int, [_vp, _vp, _int, _int, _int, _vp]),
     "gbsym_tri_solve_b": (_int, [_vp, _vp, _vp, _vp]),
@@ -115,7 +118,10 @@ OK, ERR_NULL_ARG, ERR_BAD_SCHEDULE, ERR_PIVOT, ERR_TIMEOUT, ERR_CUDA, ERR_BAD_MA
 LOWER_DIAG_LAST, UPPER_DIAG_FIRST, ILU_UNIT_LOWER, ILU_UPPER, ILU_LOWER_DIV = range(5)
 F64, F32 = 0, 1
 COL_MAJOR, ROW_MAJOR = 0, 1
-EXEC_AUTO, EXEC_LEVELSET, EXEC_SYNCFREE, EXEC_ONEBLOCK = range(4)
+EXEC_AUTO, EXEC_LEVELSET, EXEC_SYNCFREE, EXEC_ONEBLOCK, EXEC_PERSISTENT, EXEC_CLUSTER = range(6)
+EXEC_NAMES = {EXEC_LEVELSET: "levelset", EXEC_SYNCFREE: "syncfree", EXEC_ONEBLOCK: "oneblock",
+              EXEC_PERSISTENT: "persistent", EXEC_CLUSTER: "cluster"}
+ARITH_EXACT, ARITH_FUSED = 0, 1
 
 
 def check(status: int, where: str = ""):

@@ -88,6 +88,8 @@ static void tri_dropin(int n, const int *p, const int *i, const double *v, const
   upload(dx, x, n, false, s);
   if (b) upload(db, b, n, false, s);
   tri_solve_rowmajor(t.get(), dx.p, b ? db.p : nullptr, 1, GBSYM_F64, s);
+  const int code = tri_read_error(t.get(), s);
+  if (code) throw Err{code};
   GB_CUDA(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
 }
@@ -154,6 +156,8 @@ static void csc_dropin(int n, const int *Lp, const int *Li, const double *Lx, do
   DBuf<double> dx;
   upload(dx, x, n, false, s);
   tri_solve_rowmajor(t.get(), dx.p, nullptr, 1, GBSYM_F64, s);
+  const int code = tri_read_error(t.get(), s);
+  if (code) throw Err{code};
   GB_CUDA(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
 }
@@ -467,6 +471,9 @@ void gbsym_parsy_lus_cr(int n, int nz_num, int *ia, int *ja, double *l, int *ua,
     upload(dz, r, n, false, s);
     tri_solve_rowmajor(lo.get(), dz.p, nullptr, 1, GBSYM_F64, s);
     tri_solve_rowmajor(up.get(), dz.p, nullptr, 1, GBSYM_F64, s);
+    int code = tri_read_error(lo.get(), s);
+    if (!code) code = tri_read_error(up.get(), s);
+    if (code) throw Err{code};
     GB_CUDA(cudaMemcpyAsync(z, dz.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
     GB_CUDA(cudaStreamSynchronize(s));
   });

@@ -1,0 +1,180 @@
+// exec.cu -- executor dispatch, default choice and the autotuner.
+//
+// The reference has one executor per schedule kind and a fixed OpenMP
+// thread count (sptrsv_demo.cpp:36-65).  Here five GPU executors run any
+// level-packed plan (exec_level.cu, exec_sweep.cu, exec_syncfree.cu,
+// exec_cluster.cu);
+// which is fastest depends on the wavefront depth, the level width, the
+// row length, the number of right-hand sides and the arithmetic.  The
+// default choice is a heuristic; gbsym_tri_autotune times the candidates on
+// the plan itself and remembers the winner for the plan and, process-wide,
+// for plans with the same key (level count, mean row length, k, dtype).
+#include <algorithm>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
+#include "exec_common.cuh"
+
+namespace gbsym {
+
+using TuneKey = std::tuple<int, int, int, int, int>;  // levels, mean len x4, k, dtype, arith
+static std::map<TuneKey, int> g_tuned;
+static std::mutex g_tuned_mu;
+
+static TuneKey tune_key(const gbsym_tri_s *t, int k, int dtype) {
+  const int mean4 = t->n ? (int)(4.0 * (double)t->nnz_off / t->n + 0.5) : 0;
+  return TuneKey(t->nlev, mean4, std::min(k, 64), dtype, t->arith);
+}
+
+int effective_exec(const gbsym_tri_s *t, int k, bool redundant) {
+  int e = t->exec_forced != GBSYM_EXEC_AUTO ? t->exec_forced : (k == 1 ? t->exec : t->exec_mrhs);
+  if (redundant) e = GBSYM_EXEC_LEVELSET;
+  if (e == GBSYM_EXEC_ONEBLOCK && k != 1) e = GBSYM_EXEC_SYNCFREE;
+  if (t->nlev <= 1) e = GBSYM_EXEC_LEVELSET;
+  return e;
+}
+
+// Default executor before any tuning: the sync-free sweep (no level
+// barriers) unless the levels are narrow enough for one block.
+void choose_exec(gbsym_tri_s *t) {
+  const double mean_rows = (double)t->n / std::max(1, t->nlev);
+  t->exec = (t->max_level_rows <= 512 && mean_rows <= 256.0) ? GBSYM_EXEC_ONEBLOCK : GBSYM_EXEC_SYNCFREE;
+  t->exec_mrhs = GBSYM_EXEC_SYNCFREE;
+  {
+    std::lock_guard<std::mutex> lk(g_tuned_mu);
+    auto it1 = g_tuned.find(tune_key(t, 1, t->vdtype));
+    if (it1 != g_tuned.end()) t->exec = it1->second;
+  }
+  if (const char *force = std::getenv("GBSYM_TRI_EXEC")) {
+    int e = -1;
+    if (!std::strcmp(force, "levelset")) e = GBSYM_EXEC_LEVELSET;
+    else if (!std::strcmp(force, "persistent")) e = GBSYM_EXEC_PERSISTENT;
+    else if (!std::strcmp(force, "oneblock")) e = GBSYM_EXEC_ONEBLOCK;
+    else if (!std::strcmp(force, "syncfree")) e = GBSYM_EXEC_SYNCFREE;
+    else if (!std::strcmp(force, "cluster")) e = GBSYM_EXEC_CLUSTER;
+    if (e >= 0) {
+      t->exec = e;
+      t->exec_mrhs = e == GBSYM_EXEC_ONEBLOCK ? GBSYM_EXEC_SYNCFREE : e;
+    }
+  }
+  if (const char *pb = std::getenv("GBSYM_PERSIST_BLOCKS")) t->persist_blocks = std::atoi(pb);
+  if (const char *cb = std::getenv("GBSYM_CLUSTER_BLOCKS")) t->cluster_blocks = std::atoi(cb);
+}
+
+template <class T>
+static void solve_as(gbsym_tri_s *t, int e, T *x, const T *b, int k, int dtype, cudaStream_t s) {
+  switch (e) {
+    case GBSYM_EXEC_ONEBLOCK: run_oneblock<T>(t, x, s); break;
+    case GBSYM_EXEC_PERSISTENT: run_persist<T>(t, x, k, s); break;
+    case GBSYM_EXEC_SYNCFREE: run_syncfree<T>(t, x, k, s); break;
+    case GBSYM_EXEC_CLUSTER: run_cluster<T>(t, x, k, s); break;
+    default: run_levelset<T>(t, x, b, k, dtype, s); break;
+  }
+}
+
+template <class T>
+static void solve_typed(gbsym_tri_s *t, T *x, const T *b, int k, int dtype, cudaStream_t s) {
+  if (t->n == 0 || k == 0) return;
+  solve_as<T>(t, effective_exec(t, k, b != nullptr), x, b, k, dtype, s);
+}
+
+void tri_solve_rowmajor(gbsym_tri_s *t, void *x, const void *b, int k, int dtype, cudaStream_t s) {
+  if (dtype == GBSYM_F64) {
+    GB_CHECK(t->vdtype == GBSYM_F64, GBSYM_ERR_UNSUPPORTED);
+    solve_typed<double>(t, (double *)x, (const double *)b, k, dtype, s);
+  } else {
+    GB_CHECK(t->vdtype == GBSYM_F32 && b == nullptr, GBSYM_ERR_UNSUPPORTED);
+    solve_typed<float>(t, (float *)x, nullptr, k, dtype, s);
+  }
+}
+
+int tri_read_error(gbsym_tri_s *t, cudaStream_t s) {
+  int h[2] = {0, 0};
+  GB_CUDA(cudaMemcpyAsync(h, t->err.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  if (h[0]) GB_CUDA(cudaMemsetAsync(t->err.p, 0, 2 * sizeof(int), s));
+  return h[0];
+}
+
+template <class T>
+__global__ void k_fill_tune(T *x, long long m) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < m;
+       i += (long long)gridDim.x * blockDim.x)
+    x[i] = T(1) + T(i % 7) * T(0.125);
+}
+
+template <class T>
+static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
+  const long long m = (long long)t->n * k;
+  DBuf<T> buf(m);
+  std::vector<int> cands = {GBSYM_EXEC_LEVELSET, GBSYM_EXEC_PERSISTENT, GBSYM_EXEC_SYNCFREE,
+                            GBSYM_EXEC_CLUSTER};
+  if (k == 1 && t->max_level_rows <= 4096) cands.push_back(GBSYM_EXEC_ONEBLOCK);
+  cudaEvent_t e0, e1;
+  GB_CUDA(cudaEventCreate(&e0));
+  GB_CUDA(cudaEventCreate(&e1));
+  int best = -1;
+  float best_ms = 0;
+  for (int e : cands) {
+    std::vector<float> ms;
+    for (int rep = 0; rep < 4; ++rep) {
+      k_fill_tune<T><<<(int)std::min<long long>(div_up(m, 256), num_sms() * 8), 256, 0, s>>>(buf.p, m);
+      check_launch();
+      GB_CUDA(cudaEventRecord(e0, s));
+      solve_as<T>(t, e, buf.p, nullptr, k, dtype, s);
+      GB_CUDA(cudaEventRecord(e1, s));
+      GB_CUDA(cudaEventSynchronize(e1));
+      float v = 0;
+      GB_CUDA(cudaEventElapsedTime(&v, e0, e1));
+      if (rep) ms.push_back(v);  // the first run builds graphs and warms caches
+    }
+    if (tri_read_error(t, s)) continue;  // a candidate that timed out is skipped
+    std::sort(ms.begin(), ms.end());
+    const float med = ms[ms.size() / 2];
+    if (best < 0 || med < best_ms) {
+      best = e;
+      best_ms = med;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (best < 0) throw Err{GBSYM_ERR_TIMEOUT};
+  if (k == 1) t->exec = best; else t->exec_mrhs = best;
+  std::lock_guard<std::mutex> lk(g_tuned_mu);
+  g_tuned[tune_key(t, k, dtype)] = best;
+  return best;
+}
+
+}  // namespace gbsym
+
+using namespace gbsym;
+
+extern "C" int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, int *chosen) {
+  if (!t) return GBSYM_ERR_NULL_ARG;
+  if (k < 1) return GBSYM_ERR_SIZE;
+  return guarded([&] {
+    cudaStream_t s = (cudaStream_t)stream;
+    int e = GBSYM_EXEC_LEVELSET;
+    if (t->n > 0 && t->nlev > 1) {
+      if (dtype == GBSYM_F64) {
+        GB_CHECK(t->vdtype == GBSYM_F64, GBSYM_ERR_UNSUPPORTED);
+        e = autotune_typed<double>(t, k, dtype, s);
+      } else {
+        GB_CHECK(t->vdtype == GBSYM_F32, GBSYM_ERR_UNSUPPORTED);
+        e = autotune_typed<float>(t, k, dtype, s);
+      }
+    }
+    if (chosen) *chosen = e;
+  });
+}
+
+extern "C" int gbsym_tri_set_arith(gbsym_tri t, int arith) {
+  if (!t) return GBSYM_ERR_NULL_ARG;
+  if (arith != GBSYM_ARITH_EXACT && arith != GBSYM_ARITH_FUSED) return GBSYM_ERR_UNSUPPORTED;
+  t->arith = arith;
+  return GBSYM_OK;
+}

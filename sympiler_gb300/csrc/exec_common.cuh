@@ -1,0 +1,208 @@
+// exec_common.cuh -- device helpers shared by the triangular-solve
+// executors (exec_level.cu, exec_sweep.cu, exec_syncfree.cu,
+// exec_cluster.cu) and their
+// host-side entry points (exec.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "tri.cuh"
+
+namespace gbsym {
+
+// ---------------------------------------------------------------------------
+// arithmetic policies.  EXACT: x -= v*x_j as a rounded product and a rounded
+// difference (the reference's sequence); FUSED: one fused multiply-add per
+// entry (one rounding; results differ from the reference by a few ulps).
+enum { kArithExact = 0, kArithFused = 1 };
+
+template <int AR, class T>
+__device__ __forceinline__ T msub(T acc, T v, T xj) {
+  if (AR == kArithExact) return sub_rn(acc, mul_rn(v, xj));
+  if constexpr (sizeof(T) == 8) return __fma_rn(-v, xj, acc);
+  else return __fmaf_rn(-v, xj, acc);
+}
+
+// Correctly rounded a / b given y = RN(1/b).  Markstein's method (P.
+// Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990): for a faithful
+// quotient q = RN(a*y), the remainder a - q*b is exact under one fused
+// multiply-add and q + (a - q*b)*y rounds to a/b.  The theorem needs every
+// intermediate normal, so operands whose exponents could under- or
+// overflow the remainder or the quotient (and zeros, infinities, NaNs) take
+// IEEE division instead.  Three dependent FP64 operations replace a
+// division that costs about seven FMAs of issue and 280 ns of latency on
+// this part.
+__device__ __forceinline__ double div_by(double a, double b, double y) {
+  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
+  const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
+  if (ea >= 63 && ea <= 2043 && eb >= 3 && eb <= 2043 && ea - eb <= 1000 && eb - ea <= 1000) {
+    const double q = __dmul_rn(a, y);
+    const double r = __fma_rn(-q, b, a);
+    return __fma_rn(r, y, q);
+  }
+  return __ddiv_rn(a, b);
+}
+__device__ __forceinline__ float div_by(float a, float b, float /*y*/) { return __fdiv_rn(a, b); }
+
+__device__ __forceinline__ void pdl_trigger() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_add(unsigned *p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// L2-coherent loads for values other blocks write while a launch runs.
+__device__ __forceinline__ double ldx(const double *p) { return __ldcg(p); }
+__device__ __forceinline__ float ldx(const float *p) { return __ldcg(p); }
+template <class T, bool CG>
+__device__ __forceinline__ T ldv(const T *p) {
+  return CG ? ldx(p) : *p;
+}
+
+// ---------------------------------------------------------------------------
+// Static part of a row: everything that does not depend on x.  All loads
+// are independent of each other (slab entries are addressed by the packed
+// row index alone), so they are in flight together.
+template <class T>
+struct RowStatic {
+  int orig, len, ovb;
+  T d, y;
+  int c[kSlabMax];
+  T v[kSlabMax];
+};
+
+template <class T>
+__device__ __forceinline__ void load_row(const TriView<T> &A, int row, RowStatic<T> &r) {
+  r.orig = A.perm[row];
+  r.len = A.len[row];
+  r.d = A.dg ? A.dg[row] : T(1);
+  r.y = A.dg ? A.rc[row] : T(1);
+  r.ovb = A.ovp ? A.ovp[row] : 0;
+#pragma unroll
+  for (int q = 0; q < kSlabMax; ++q)
+    if (q < A.K) {
+      r.c[q] = A.sci[(size_t)q * A.npad + row];
+      r.v[q] = A.sv[(size_t)q * A.npad + row];
+    }
+}
+
+// acc - sum_q v_q x[c_q] in storage order; the slab gathers are issued
+// together before the first subtraction.
+template <class T, bool CG, int AR>
+__device__ __forceinline__ T row_accumulate(const TriView<T> &A, const RowStatic<T> &r, const T *x,
+                                            T acc) {
+  T xv[kSlabMax];
+#pragma unroll
+  for (int q = 0; q < kSlabMax; ++q)
+    if (q < A.K && q < r.len) xv[q] = ldv<T, CG>(x + r.c[q]);
+#pragma unroll
+  for (int q = 0; q < kSlabMax; ++q)
+    if (q < A.K && q < r.len) acc = msub<AR>(acc, r.v[q], xv[q]);
+  for (int t = A.K; t < r.len; ++t) {
+    const int e = r.ovb + t - A.K;
+    acc = msub<AR>(acc, A.ov[e], ldv<T, CG>(x + A.oci[e]));
+  }
+  return acc;
+}
+
+template <class T>
+__device__ __forceinline__ T row_finish(const TriView<T> &A, const RowStatic<T> &r, T acc) {
+  return A.dg ? div_by(acc, r.d, r.y) : acc;
+}
+
+template <class T, int VEC> struct VecT;
+template <> struct VecT<double, 1> { using t = double; };
+template <> struct VecT<double, 2> { using t = double2; };
+template <> struct VecT<float, 1> { using t = float; };
+template <> struct VecT<float, 2> { using t = float2; };
+template <> struct VecT<float, 4> { using t = float4; };
+
+template <class T, int VEC, bool CG>
+__device__ __forceinline__ void vload(const T *p, T (&v)[VEC]) {
+  using V = typename VecT<T, VEC>::t;
+  const V t = CG ? __ldcg(reinterpret_cast<const V *>(p)) : *reinterpret_cast<const V *>(p);
+  const T *s = reinterpret_cast<const T *>(&t);
+#pragma unroll
+  for (int q = 0; q < VEC; ++q) v[q] = s[q];
+}
+template <class T, int VEC>
+__device__ __forceinline__ void vstore(T *p, const T (&v)[VEC]) {
+  using V = typename VecT<T, VEC>::t;
+  V t;
+  T *s = reinterpret_cast<T *>(&t);
+#pragma unroll
+  for (int q = 0; q < VEC; ++q) s[q] = v[q];
+  *reinterpret_cast<V *>(p) = t;
+}
+
+// k right-hand sides of one row, row-major x[i*k + r]: this lane's VEC-wide
+// slices r = lane*VEC, lane*VEC + G*VEC, ...; all slab gathers of a slice
+// are issued before the in-order accumulation.
+template <class T, int G, int VEC, bool CG, int AR>
+__device__ __forceinline__ void row_mrhs(const TriView<T> &A, const RowStatic<T> &rs, T *x, int k,
+                                         int lane) {
+  const size_t orig = (size_t)rs.orig;
+  for (int r = lane * VEC; r < k; r += G * VEC) {
+    T acc[VEC];
+    vload<T, VEC, CG>(x + orig * k + r, acc);
+    T xv[kSlabMax][VEC];
+#pragma unroll
+    for (int q = 0; q < kSlabMax; ++q)
+      if (q < A.K && q < rs.len) vload<T, VEC, CG>(x + (size_t)rs.c[q] * k + r, xv[q]);
+#pragma unroll
+    for (int q = 0; q < kSlabMax; ++q)
+      if (q < A.K && q < rs.len) {
+#pragma unroll
+        for (int u = 0; u < VEC; ++u) acc[u] = msub<AR>(acc[u], rs.v[q], xv[q][u]);
+      }
+    for (int t = A.K; t < rs.len; ++t) {
+      const int e = rs.ovb + t - A.K;
+      const T v = A.ov[e];
+      T y[VEC];
+      vload<T, VEC, CG>(x + (size_t)A.oci[e] * k + r, y);
+#pragma unroll
+      for (int u = 0; u < VEC; ++u) acc[u] = msub<AR>(acc[u], v, y[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < VEC; ++u) acc[u] = row_finish(A, rs, acc[u]);
+    vstore<T, VEC>(x + orig * k + r, acc);
+  }
+}
+
+// lanes per row: enough to cover k with 2-wide (FP64) / 4-wide (FP32) loads
+inline int lanes_for(int k, int dsize) {
+  const int per = dsize == 8 ? 2 : 4;
+  const int need = div_up(k, per);
+  int g = 2;
+  while (g < need && g < 32) g <<= 1;
+  return g;
+}
+
+template <class T>
+inline TriView<T> view_of(const gbsym_tri_s *t);
+template <>
+inline TriView<double> view_of<double>(const gbsym_tri_s *t) { return t->view64(); }
+template <>
+inline TriView<float> view_of<float>(const gbsym_tri_s *t) { return t->view32(); }
+
+// Host entry points of the executors (one translation unit each).
+template <class T>
+void run_levelset(gbsym_tri_s *t, T *x, const T *b, int k, int dtype, cudaStream_t s);
+template <class T>
+void run_persist(gbsym_tri_s *t, T *x, int k, cudaStream_t s);
+template <class T>
+void run_oneblock(gbsym_tri_s *t, T *x, cudaStream_t s);
+template <class T>
+void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s);
+template <class T>
+void run_cluster(gbsym_tri_s *t, T *x, int k, cudaStream_t s);
+
+}  // namespace gbsym

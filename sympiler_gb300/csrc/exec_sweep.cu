@@ -1,0 +1,213 @@
+// exec_sweep.cu -- PERSISTENT and ONEBLOCK executors: one launch sweeps all
+// wavefront levels.
+//
+// PERSISTENT: a cooperative launch (every block co-resident); levels are
+// separated by a bounded grid barrier -- one release-add per block, acquire
+// polling -- and each thread loads the static part of its next row before
+// it enters the barrier.  ONEBLOCK: the same sweep in a single block, where
+// __syncthreads is the barrier and x is staged in shared memory when it
+// fits; it suits systems whose levels are a few hundred rows wide.
+#include <algorithm>
+
+#include "exec_common.cuh"
+
+namespace gbsym {
+
+// Grid barrier: every block adds 1 with release semantics after its
+// stores, then polls with acquire until all blocks of generation `target`
+// have arrived.  Returns false (and records GBSYM_ERR_TIMEOUT) when the
+// wait runs out, after which every block leaves the sweep.
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target, int *err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    red_release_add(bar, 1u);
+    int ok = 1;
+    long long it = 0;
+    const unsigned long long t0 = globaltimer_ns();
+    while ((int)(ld_acquire_u32(bar) - target) < 0) {
+      ++it;
+      if (it > kWaitLimitIters || ((it & 255) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) ||
+          ((it & 255) == 0 && ld_relaxed(err) != 0)) {
+        atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
+        ok = 0;
+        break;
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+constexpr int kPersistBlock = 256;
+constexpr int kOneBlock = 512;
+
+template <class T, bool ONE_BLOCK, int AR>
+__global__ void __launch_bounds__(ONE_BLOCK ? kOneBlock : kPersistBlock)
+k_sweep_1rhs(TriView<T> A, T *__restrict__ xg, const int *__restrict__ lev_ptr, int nlev, int n,
+             int xs_smem, unsigned *bar, int *err) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *x = (ONE_BLOCK && xs_smem) ? reinterpret_cast<T *>(smem_raw) : xg;
+  if (ONE_BLOCK && xs_smem) {
+    for (int i = threadIdx.x; i < n; i += blockDim.x) x[i] = xg[i];
+    __syncthreads();
+  }
+  constexpr bool CG = !ONE_BLOCK;
+  const int nthr = gridDim.x * blockDim.x;
+  const int gtid = blockIdx.x * blockDim.x + threadIdx.x;
+  RowStatic<T> rs;
+  int r0 = lev_ptr[0], r1 = lev_ptr[1];
+  if (r0 + gtid < r1) load_row(A, r0 + gtid, rs);
+  for (int l = 0; l < nlev; ++l) {
+    int row = r0 + gtid;
+    if (row < r1) {
+      T acc = ldv<T, CG>(x + rs.orig);
+      acc = row_accumulate<T, CG, AR>(A, rs, x, acc);
+      x[rs.orig] = row_finish(A, rs, acc);
+    }
+    for (row += nthr; row < r1; row += nthr) {
+      RowStatic<T> r2;
+      load_row(A, row, r2);
+      T acc = ldv<T, CG>(x + r2.orig);
+      acc = row_accumulate<T, CG, AR>(A, r2, x, acc);
+      x[r2.orig] = row_finish(A, r2, acc);
+    }
+    if (l + 1 < nlev) {
+      const int n0 = r1, n1 = lev_ptr[l + 2];
+      if (n0 + gtid < n1) load_row(A, n0 + gtid, rs);
+      if (ONE_BLOCK) {
+        __syncthreads();
+      } else if (!grid_barrier(bar, (unsigned)(l + 1) * gridDim.x, err)) {
+        return;
+      }
+      r0 = n0;
+      r1 = n1;
+    }
+  }
+  if (ONE_BLOCK && xs_smem) {
+    __syncthreads();
+    for (int i = threadIdx.x; i < n; i += blockDim.x) xg[i] = x[i];
+  }
+}
+
+template <class T, int G, int VEC, int AR>
+__global__ void __launch_bounds__(kPersistBlock)
+k_sweep_mrhs(TriView<T> A, T *__restrict__ x, int k, const int *__restrict__ lev_ptr, int nlev,
+             unsigned *bar, int *err) {
+  const int ngroups = gridDim.x * blockDim.x / G;
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int lane = threadIdx.x % G;
+  RowStatic<T> rs;
+  int r0 = lev_ptr[0], r1 = lev_ptr[1];
+  if (r0 + gid < r1) load_row(A, r0 + gid, rs);
+  for (int l = 0; l < nlev; ++l) {
+    int row = r0 + gid;
+    if (row < r1) row_mrhs<T, G, VEC, true, AR>(A, rs, x, k, lane);
+    for (row += ngroups; row < r1; row += ngroups) {
+      RowStatic<T> r2;
+      load_row(A, row, r2);
+      row_mrhs<T, G, VEC, true, AR>(A, r2, x, k, lane);
+    }
+    if (l + 1 < nlev) {
+      const int n0 = r1, n1 = lev_ptr[l + 2];
+      if (n0 + gid < n1) load_row(A, n0 + gid, rs);
+      if (!grid_barrier(bar, (unsigned)(l + 1) * gridDim.x, err)) return;
+      r0 = n0;
+      r1 = n1;
+    }
+  }
+}
+
+static size_t oneblock_smem(const gbsym_tri_s *t, int dsize) {
+  const size_t need = (size_t)t->n * dsize;
+  return need <= 200 * 1024 ? need : 0;
+}
+
+template <class T, int AR>
+static void oneblock_ar(gbsym_tri_s *t, T *x, cudaStream_t s) {
+  const size_t sm = oneblock_smem(t, sizeof(T));
+  auto kern = k_sweep_1rhs<T, true, AR>;
+  if (sm > 48 * 1024)
+    GB_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+  kern<<<1, kOneBlock, sm, s>>>(view_of<T>(t), x, t->lev_ptr.p, t->nlev, t->n, sm > 0 ? 1 : 0, t->bar.p,
+                                t->err.p);
+  check_launch();
+}
+
+template <class T>
+void run_oneblock(gbsym_tri_s *t, T *x, cudaStream_t s) {
+  if (t->arith == kArithFused) oneblock_ar<T, kArithFused>(t, x, s);
+  else oneblock_ar<T, kArithExact>(t, x, s);
+}
+
+// Grid of the persistent sweep: enough groups to cover the widest level,
+// bounded by what is co-resident (the cooperative launch checks it).
+template <class K>
+static int persist_grid(gbsym_tri_s *t, K kernel, int lanes_per_row) {
+  int per_sm = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kPersistBlock, 0));
+  const int cap = std::max(1, per_sm) * num_sms();
+  const long long want = div_up((long long)t->max_level_rows * lanes_per_row, kPersistBlock);
+  int g = (int)std::min<long long>(cap, std::max<long long>(1, want));
+  if (t->persist_blocks > 0) g = std::min(g, t->persist_blocks);
+  return g;
+}
+
+template <class K, class... Args>
+static void launch_coop(K kernel, int grid, cudaStream_t s, Args... args) {
+  void *params[] = {(void *)&args...};
+  GB_CUDA(cudaLaunchCooperativeKernel((const void *)kernel, dim3(grid), dim3(kPersistBlock), params, 0, s));
+  check_launch();
+}
+
+template <class T, int G, int AR>
+static void persist_mrhs_g(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
+  const TriView<T> A = view_of<T>(t);
+  const int *lp = t->lev_ptr.p;
+  const bool v4 = sizeof(T) == 4 && (k % 4 == 0) && ((uintptr_t)x % 16 == 0);
+  const bool v2 = (k % 2 == 0) && ((uintptr_t)x % (2 * sizeof(T)) == 0);
+  if (v4) {
+    auto kern = k_sweep_mrhs<T, G, (sizeof(T) == 4 ? 4 : 2), AR>;
+    launch_coop(kern, persist_grid(t, kern, G), s, A, x, k, lp, t->nlev, t->bar.p, t->err.p);
+  } else if (v2) {
+    auto kern = k_sweep_mrhs<T, G, 2, AR>;
+    launch_coop(kern, persist_grid(t, kern, G), s, A, x, k, lp, t->nlev, t->bar.p, t->err.p);
+  } else {
+    auto kern = k_sweep_mrhs<T, G, 1, AR>;
+    launch_coop(kern, persist_grid(t, kern, G), s, A, x, k, lp, t->nlev, t->bar.p, t->err.p);
+  }
+}
+
+template <class T, int AR>
+static void persist_ar(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
+  if (k == 1) {
+    auto kern = k_sweep_1rhs<T, false, AR>;
+    launch_coop(kern, persist_grid(t, kern, 1), s, view_of<T>(t), x, (const int *)t->lev_ptr.p, t->nlev,
+                t->n, 0, t->bar.p, t->err.p);
+    return;
+  }
+  switch (lanes_for(k, sizeof(T))) {
+    case 2: persist_mrhs_g<T, 2, AR>(t, x, k, s); break;
+    case 4: persist_mrhs_g<T, 4, AR>(t, x, k, s); break;
+    case 8: persist_mrhs_g<T, 8, AR>(t, x, k, s); break;
+    case 16: persist_mrhs_g<T, 16, AR>(t, x, k, s); break;
+    default: persist_mrhs_g<T, 32, AR>(t, x, k, s); break;
+  }
+}
+
+template <class T>
+void run_persist(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
+  GB_CUDA(cudaMemsetAsync(t->bar.p, 0, sizeof(unsigned), s));
+  count_launch();
+  if (t->arith == kArithFused) persist_ar<T, kArithFused>(t, x, k, s);
+  else persist_ar<T, kArithExact>(t, x, k, s);
+}
+
+template void run_oneblock<double>(gbsym_tri_s *, double *, cudaStream_t);
+template void run_oneblock<float>(gbsym_tri_s *, float *, cudaStream_t);
+template void run_persist<double>(gbsym_tri_s *, double *, int, cudaStream_t);
+template void run_persist<float>(gbsym_tri_s *, float *, int, cudaStream_t);
+
+}  // namespace gbsym

@@ -331,342 +331,106 @@ void validate_lbc(int n, const int *d_p, const int *d_i, const int *d_diags, int
 // ---------------------------------------------------------------------------
 // packing
 __global__ void k_pack_counts(int n, const int *__restrict__ perm, const int *__restrict__ p,
-                              const int *__restrict__ diags, int kind, int *cnt, int *maxcnt) {
-  int m = 0;
-  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= n; k += gridDim.x * blockDim.x) {
-    if (k == n) { cnt[k] = 0; continue; }
+                              const int *__restrict__ diags, int kind, int *len, int *hist) {
+  __shared__ int sh[kSlabMax + 2];
+  if (threadIdx.x < kSlabMax + 2) sh[threadIdx.x] = 0;
+  __syncthreads();
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
     const RowDef r = row_def(kind, p, diags, perm[k]);
-    cnt[k] = r.hi - r.lo;
-    m = max(m, r.hi - r.lo);
+    const int c = r.hi - r.lo;
+    len[k] = c;
+    atomicAdd(&sh[min(c, kSlabMax + 1)], 1);
   }
-  for (int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-  if ((threadIdx.x & 31) == 0) atomicMax(maxcnt, m);
+  __syncthreads();
+  if (threadIdx.x < kSlabMax + 2) atomicAdd(&hist[threadIdx.x], sh[threadIdx.x]);
+}
+
+__global__ void k_overflow_counts(int n, const int *__restrict__ len, int K, int *cnt) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k <= n; k += gridDim.x * blockDim.x)
+    cnt[k] = k < n ? max(0, len[k] - K) : 0;
 }
 
 template <class V>
 __global__ void k_pack_rows(int n, const int *__restrict__ perm, const int *__restrict__ p,
                             const int *__restrict__ ci_in, const double *__restrict__ x_in,
-                            const int *__restrict__ diags, int kind, const int *__restrict__ rp,
-                            int *ci_out, V *val_out, V *dg_out) {
+                            const int *__restrict__ diags, int kind, int K, int npad,
+                            const int *__restrict__ ovp, int *sci, V *sv, int *oci, V *ov, V *dg) {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int k = warp; k < n; k += nwarps) {
     const RowDef r = row_def(kind, p, diags, perm[k]);
-    const int base = rp[k];
-    for (int t = lane; t < r.hi - r.lo; t += 32) {
-      ci_out[base + t] = ci_in[r.lo + t];
-      val_out[base + t] = (V)x_in[r.lo + t];
+    const int c = r.hi - r.lo;
+    for (int t = lane; t < max(c, K); t += 32) {
+      if (t < K) {  // slab slots past the row's length hold a harmless zero entry
+        sci[(size_t)t * npad + k] = t < c ? ci_in[r.lo + t] : 0;
+        sv[(size_t)t * npad + k] = t < c ? (V)x_in[r.lo + t] : (V)0;
+      } else {
+        oci[ovp[k] + t - K] = ci_in[r.lo + t];
+        ov[ovp[k] + t - K] = (V)x_in[r.lo + t];
+      }
     }
-    if (lane == 0) dg_out[k] = r.dpos >= 0 ? (V)x_in[r.dpos] : (V)1;
+    if (lane == 0) dg[k] = r.dpos >= 0 ? (V)x_in[r.dpos] : (V)1;
   }
 }
 
-// ---------------------------------------------------------------------------
-// executors
-constexpr int kLvlBlock = 128;   // rows per block, one thread per row
-constexpr int kLvlChunk = 1024;  // staged entries per pass
-
-// One level, one right-hand side.  The level's packed row block
-// [r0, r1) is staged chunk by chunk into shared memory with coalesced
-// loads, then each thread accumulates its row in storage order.
-template <class T, bool REDUNDANT>
-__global__ void __launch_bounds__(kLvlBlock)
-k_level_1rhs(TriView<T> A, T *__restrict__ x, const T *__restrict__ b, int r_begin, int r_end) {
-  __shared__ int s_ci[kLvlChunk];
-  __shared__ T s_v[kLvlChunk];
-  const int r0 = r_begin + blockIdx.x * kLvlBlock;
-  const int r1 = min(r0 + kLvlBlock, r_end);
-  const int row = r0 + threadIdx.x;
-  const bool active = row < r1;
-  const int e0 = A.rp[r0], e1 = A.rp[r1];
-  int lo = 0, hi = 0, orig = 0;
-  T acc = T(0);
-  if (active) {
-    lo = A.rp[row];
-    hi = A.rp[row + 1];
-    orig = A.perm[row];
-    if (!REDUNDANT) acc = x[orig];
-  }
-  for (int c0 = e0; c0 < e1; c0 += kLvlChunk) {
-    const int c1 = min(c0 + kLvlChunk, e1);
-    if (c0 != e0) __syncthreads();
-    for (int e = c0 + threadIdx.x; e < c1; e += kLvlBlock) {
-      s_ci[e - c0] = A.ci[e];
-      s_v[e - c0] = A.val[e];
+// Slab width: the K in [0, kSlabMax] with the fewest bytes (slab slots
+// plus overflow entries plus overflow pointers), preferring a wider slab
+// while it costs at most a quarter more -- entries in the slab are loaded
+// before a level kernel waits on its predecessor, overflow entries after.
+static int choose_slab_width(int n, const int *hist) {
+  long long best_cost = -1;
+  int bestK = 0;
+  long long cost[kSlabMax + 1];
+  for (int K = 0; K <= kSlabMax; ++K) {
+    long long over = 0, rows_over = 0;
+    for (int c = K + 1; c <= kSlabMax; ++c) {
+      over += (long long)(c - K) * hist[c];
+      rows_over += hist[c];
     }
-    __syncthreads();
-    if (active) {
-      const int a = max(lo, c0), z = min(hi, c1);
-      for (int e = a; e < z; ++e) acc = sub_rn(acc, mul_rn(s_v[e - c0], x[s_ci[e - c0]]));
+    // rows longer than kSlabMax: their excess is counted at kSlabMax + 1
+    over += (long long)(kSlabMax + 1 - K) * hist[kSlabMax + 1];
+    rows_over += hist[kSlabMax + 1];
+    cost[K] = (long long)K * n + over + (rows_over ? n : 0);
+    if (best_cost < 0 || cost[K] < best_cost) {
+      best_cost = cost[K];
+      bestK = K;
     }
   }
-  if (active) {
-    if (REDUNDANT) acc = add_rn(acc, b[orig]);
-    if (A.dg) acc = div_rn(acc, A.dg[row]);
-    x[orig] = acc;
-  }
+  int K = bestK;
+  for (int c = kSlabMax; c > bestK; --c)
+    if (cost[c] * 4 <= best_cost * 5) {
+      K = c;
+      break;
+    }
+  return K;
 }
 
-// One level, k right-hand sides stored row-major (x[i*k + r]).  G lanes
-// share a row; each lane owns VEC consecutive right-hand sides per step, so
-// a dependency's k values are read as one coalesced segment.
-template <class T, int VEC> struct VecT;
-template <> struct VecT<double, 1> { using t = double; };
-template <> struct VecT<double, 2> { using t = double2; };
-template <> struct VecT<float, 1> { using t = float; };
-template <> struct VecT<float, 2> { using t = float2; };
-template <> struct VecT<float, 4> { using t = float4; };
+__device__ __forceinline__ double rcp_rn(double v) { return __drcp_rn(v); }
+__device__ __forceinline__ float rcp_rn(float v) { return __frcp_rn(v); }
 
-template <class T, int VEC>
-__device__ __forceinline__ void vload(const T *p, T (&v)[VEC]) {
-  using V = typename VecT<T, VEC>::t;
-  const V t = *reinterpret_cast<const V *>(p);
-  const T *s = reinterpret_cast<const T *>(&t);
-#pragma unroll
-  for (int q = 0; q < VEC; ++q) v[q] = s[q];
-}
-template <class T, int VEC>
-__device__ __forceinline__ void vstore(T *p, const T (&v)[VEC]) {
-  using V = typename VecT<T, VEC>::t;
-  V t;
-  T *s = reinterpret_cast<T *>(&t);
-#pragma unroll
-  for (int q = 0; q < VEC; ++q) s[q] = v[q];
-  *reinterpret_cast<V *>(p) = t;
+template <class V>
+__global__ void k_reciprocals(int n, const V *__restrict__ dg, V *rc) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    rc[k] = rcp_rn(dg[k]);
 }
 
-template <class T, int G, int VEC>
-__global__ void __launch_bounds__(256)
-k_level_mrhs(TriView<T> A, T *__restrict__ x, int k, int r_begin, int r_end) {
-  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / G;
-  const int lane = threadIdx.x % G;
-  const int row = r_begin + gid;
-  if (row >= r_end) return;
-  const int lo = A.rp[row], hi = A.rp[row + 1];
-  const size_t orig = (size_t)A.perm[row];
-  const T d = A.dg ? A.dg[row] : T(1);
-  for (int r = lane * VEC; r < k; r += G * VEC) {
-    T acc[VEC];
-    vload<T, VEC>(x + orig * k + r, acc);
-    for (int e = lo; e < hi; ++e) {
-      const T v = A.val[e];
-      T xv[VEC];
-      vload<T, VEC>(x + (size_t)A.ci[e] * k + r, xv);
-#pragma unroll
-      for (int q = 0; q < VEC; ++q) acc[q] = sub_rn(acc[q], mul_rn(v, xv[q]));
-    }
-    if (A.dg) {
-#pragma unroll
-      for (int q = 0; q < VEC; ++q) acc[q] = div_rn(acc[q], d);
-    }
-    vstore<T, VEC>(x + orig * k + r, acc);
-  }
-}
-
-// Whole solve in one thread block: levels are separated by __syncthreads.
-// x lives in shared memory when it fits (xs != x), otherwise in global
-// memory (stores of this block are visible to its own threads after the
-// barrier).  The next level's row data is loaded into registers before the
-// barrier so only the gathers of x sit on the dependency chain.
-constexpr int kOneBlock = 1024;
-constexpr int kOnePf = 8;  // prefetched entries per row
-
-template <class T>
-__global__ void __launch_bounds__(kOneBlock)
-k_oneblock_1rhs(TriView<T> A, T *__restrict__ xg, const int *__restrict__ lev_ptr, int nlev,
-                int n, int x_in_smem) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *xs = x_in_smem ? reinterpret_cast<T *>(smem_raw) : xg;
-  if (x_in_smem) {
-    for (int i = threadIdx.x; i < n; i += kOneBlock) xs[i] = xg[i];
-    __syncthreads();
-  }
-  // prefetch state for the row this thread handles first in the level
-  int lo = 0, hi = 0, orig = 0;
-  int pci[kOnePf];
-  T pv[kOnePf];
-  T pd = T(1);
-  auto prefetch = [&](int row) {
-    lo = A.rp[row];
-    hi = A.rp[row + 1];
-    orig = A.perm[row];
-    pd = A.dg ? A.dg[row] : T(1);
-#pragma unroll
-    for (int q = 0; q < kOnePf; ++q) {
-      if (lo + q < hi) { pci[q] = A.ci[lo + q]; pv[q] = A.val[lo + q]; }
-    }
-  };
-  int r0 = lev_ptr[0], r1 = nlev > 0 ? lev_ptr[1] : 0;
-  if (threadIdx.x < r1 - r0) prefetch(r0 + threadIdx.x);
-  for (int l = 0; l < nlev; ++l) {
-    const int nr0 = r1;
-    const int nr1 = (l + 1 < nlev) ? lev_ptr[l + 2] : nr0;
-    // first row of this thread in level l (prefetched)
-    int row = r0 + threadIdx.x;
-    if (row < r1) {
-      T acc = xs[orig];
-#pragma unroll
-      for (int q = 0; q < kOnePf; ++q)
-        if (lo + q < hi) acc = sub_rn(acc, mul_rn(pv[q], xs[pci[q]]));
-      for (int e = lo + kOnePf; e < hi; ++e) acc = sub_rn(acc, mul_rn(A.val[e], xs[A.ci[e]]));
-      if (A.dg) acc = div_rn(acc, pd);
-      xs[orig] = acc;
-    }
-    // remaining rows of a wide level
-    for (row += kOneBlock; row < r1; row += kOneBlock) {
-      const int a = A.rp[row], z = A.rp[row + 1], o = A.perm[row];
-      T acc = xs[o];
-      for (int e = a; e < z; ++e) acc = sub_rn(acc, mul_rn(A.val[e], xs[A.ci[e]]));
-      if (A.dg) acc = div_rn(acc, A.dg[row]);
-      xs[o] = acc;
-    }
-    if (threadIdx.x < nr1 - nr0) prefetch(nr0 + threadIdx.x);
-    r0 = nr0;
-    r1 = nr1;
-    __syncthreads();
-  }
-  if (x_in_smem) {
-    for (int i = threadIdx.x; i < n; i += kOneBlock) xg[i] = xs[i];
-  }
-}
-
-template <class T>
-static TriView<T> view_of(const gbsym_tri_s *t);
-template <>
-TriView<double> view_of<double>(const gbsym_tri_s *t) { return t->view64(); }
-template <>
-TriView<float> view_of<float>(const gbsym_tri_s *t) { return t->view32(); }
-
-template <class T, int G>
-static void launch_mrhs_g(const TriView<T> &A, T *x, int k, int a, int z, cudaStream_t s) {
-  const int rows = z - a;
-  const int rows_per_block = 256 / G;
-  const int grid = div_up(rows, rows_per_block);
-  const bool v4 = sizeof(T) == 4 && (k % 4 == 0) && ((uintptr_t)x % 16 == 0);
-  const bool v2 = (k % 2 == 0) && ((uintptr_t)x % (2 * sizeof(T)) == 0);
-  if (sizeof(T) == 4 && v4)
-    k_level_mrhs<T, G, (sizeof(T) == 4 ? 4 : 2)><<<grid, 256, 0, s>>>(A, x, k, a, z);
-  else if (v2)
-    k_level_mrhs<T, G, 2><<<grid, 256, 0, s>>>(A, x, k, a, z);
-  else
-    k_level_mrhs<T, G, 1><<<grid, 256, 0, s>>>(A, x, k, a, z);
+template <class V>
+static void pack_values(gbsym_tri_s *t, const int *d_p, const int *d_i, const double *d_x,
+                        const int *d_diags, DBuf<V> &sv, DBuf<V> &ov, DBuf<V> &dg, DBuf<V> &rc,
+                        cudaStream_t s) {
+  const int n = t->n;
+  sv.alloc((size_t)t->K * t->npad);
+  ov.alloc(t->nov);
+  dg.alloc(n);
+  rc.alloc(n);
+  if (!n) return;
+  const int gw = std::max(1, std::min(div_up(n, 8), num_sms() * 16));
+  k_pack_rows<V><<<gw, 256, 0, s>>>(n, t->perm.p, d_p, d_i, d_x, d_diags, t->kind, t->K, t->npad,
+                                    t->ovp.p, t->sci.p, sv.p, t->oci.p, ov.p, dg.p);
   check_launch();
-}
-
-template <class T>
-static void launch_level(const TriView<T> &A, T *x, const T *b, int k, int a, int z,
-                         cudaStream_t s) {
-  if (z <= a) return;
-  if (k == 1) {
-    const int grid = div_up(z - a, kLvlBlock);
-    if (b)
-      k_level_1rhs<T, true><<<grid, kLvlBlock, 0, s>>>(A, x, b, a, z);
-    else
-      k_level_1rhs<T, false><<<grid, kLvlBlock, 0, s>>>(A, x, nullptr, a, z);
-    check_launch();
-    return;
-  }
-  // lanes per row: enough to cover k with 2-wide (FP64) / 4-wide (FP32) loads
-  const int per = sizeof(T) == 8 ? 2 : 4;
-  const int need = div_up(k, per);
-  if (need <= 2) launch_mrhs_g<T, 2>(A, x, k, a, z, s);
-  else if (need <= 4) launch_mrhs_g<T, 4>(A, x, k, a, z, s);
-  else if (need <= 8) launch_mrhs_g<T, 8>(A, x, k, a, z, s);
-  else if (need <= 16) launch_mrhs_g<T, 16>(A, x, k, a, z, s);
-  else launch_mrhs_g<T, 32>(A, x, k, a, z, s);
-}
-
-template <class T>
-static void issue_levels(gbsym_tri_s *t, T *x, const T *b, int k, cudaStream_t s) {
-  const TriView<T> A = view_of<T>(t);
-  for (int l = 0; l < t->nlev; ++l) launch_level<T>(A, x, b, k, t->h_lev_ptr[l], t->h_lev_ptr[l + 1], s);
-}
-
-static size_t oneblock_smem(const gbsym_tri_s *t, int dsize) {
-  const size_t need = (size_t)t->n * dsize;
-  return need <= 200 * 1024 ? need : 0;
-}
-
-template <class T>
-static void issue_oneblock(gbsym_tri_s *t, T *x, cudaStream_t s) {
-  const size_t sm = oneblock_smem(t, sizeof(T));
-  if (sm > 48 * 1024)
-    GB_CUDA(cudaFuncSetAttribute(k_oneblock_1rhs<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)sm));
-  k_oneblock_1rhs<T><<<1, kOneBlock, sm, s>>>(view_of<T>(t), x, t->lev_ptr.p, t->nlev, t->n,
-                                              sm > 0 ? 1 : 0);
+  k_reciprocals<V><<<std::min(div_up(n, 256), num_sms() * 8), 256, 0, s>>>(n, dg.p, rc.p);
   check_launch();
-}
-
-static int effective_exec(const gbsym_tri_s *t, int k, bool redundant) {
-  int e = t->exec_forced != GBSYM_EXEC_AUTO ? t->exec_forced : t->exec;
-  if (e == GBSYM_EXEC_ONEBLOCK && (k != 1 || redundant)) e = GBSYM_EXEC_LEVELSET;
-  if (e == GBSYM_EXEC_SYNCFREE) e = GBSYM_EXEC_LEVELSET;  // not built for this path yet
-  return e;
-}
-
-// Level launches are captured once per (x, b, k, dtype) into a CUDA graph
-// and replayed; the plan keeps the eight most recent.
-template <class T>
-static void run_levelset_graph(gbsym_tri_s *t, T *x, const T *b, int k, int dtype, cudaStream_t s) {
-  GraphEntry *hit = nullptr;
-  for (auto &g : t->graphs)
-    if (g.x == x && g.b == b && g.k == k && g.dtype == dtype) hit = &g;
-  if (!hit) {
-    if (t->graphs.size() >= 8) {
-      auto old = std::min_element(t->graphs.begin(), t->graphs.end(),
-                                  [](const GraphEntry &a, const GraphEntry &c) { return a.stamp < c.stamp; });
-      cudaGraphExecDestroy(old->exec_graph);
-      t->graphs.erase(old);
-    }
-    GraphEntry g;
-    g.x = x; g.b = b; g.k = k; g.dtype = dtype;
-    cudaGraph_t graph;
-    GB_CUDA(cudaStreamBeginCapture(t->cap_stream, cudaStreamCaptureModeThreadLocal));
-    const unsigned long long before = g_launches.load();
-    try {
-      issue_levels<T>(t, x, b, k, t->cap_stream);
-    } catch (...) {
-      cudaStreamEndCapture(t->cap_stream, &graph);
-      throw;
-    }
-    g.nodes = g_launches.load() - before;
-    g_launches.fetch_sub(g.nodes);  // counted when replayed
-    GB_CUDA(cudaStreamEndCapture(t->cap_stream, &graph));
-    GB_CUDA(cudaGraphInstantiate(&g.exec_graph, graph, 0));
-    cudaGraphDestroy(graph);
-    t->graphs.push_back(g);
-    hit = &t->graphs.back();
-  }
-  hit->stamp = ++t->graph_clock;
-  GB_CUDA(cudaGraphLaunch(hit->exec_graph, s));
-  count_launch(hit->nodes);
-}
-
-template <class T>
-static void solve_typed(gbsym_tri_s *t, T *x, const T *b, int k, int dtype, cudaStream_t s) {
-  if (t->n == 0 || k == 0) return;
-  const int e = effective_exec(t, k, b != nullptr);
-  if (e == GBSYM_EXEC_ONEBLOCK) {
-    issue_oneblock<T>(t, x, s);
-    return;
-  }
-  if (t->nlev <= 2) {
-    issue_levels<T>(t, x, b, k, s);
-    return;
-  }
-  run_levelset_graph<T>(t, x, b, k, dtype, s);
-}
-
-void tri_solve_rowmajor(gbsym_tri_s *t, void *x, const void *b, int k, int dtype, cudaStream_t s) {
-  if (dtype == GBSYM_F64) {
-    GB_CHECK(t->vdtype == GBSYM_F64, GBSYM_ERR_UNSUPPORTED);
-    solve_typed<double>(t, (double *)x, (const double *)b, k, dtype, s);
-  } else {
-    GB_CHECK(t->vdtype == GBSYM_F32 && b == nullptr, GBSYM_ERR_UNSUPPORTED);
-    solve_typed<float>(t, (float *)x, nullptr, k, dtype, s);
-  }
 }
 
 // ---------------------------------------------------------------------------
@@ -707,47 +471,52 @@ gbsym_tri_s *tri_build(int n, const int *d_p, const int *d_i, const double *d_x,
   t->perm = std::move(lset);
   for (int l = 0; l < t->nlev; ++l)
     t->max_level_rows = std::max(t->max_level_rows, t->h_lev_ptr[l + 1] - t->h_lev_ptr[l]);
-  // pack
-  t->rp.alloc(n + 1);
-  DBuf<int> maxcnt(1);
-  GB_CUDA(cudaMemsetAsync(maxcnt.p, 0, sizeof(int), s));
+  // pack: lengths and the slab-width histogram, overflow pointers, values
+  t->len.alloc(n);
+  DBuf<int> hist(kSlabMax + 2);
+  GB_CUDA(cudaMemsetAsync(hist.p, 0, (kSlabMax + 2) * sizeof(int), s));
   const int g = std::max(1, std::min(div_up(n + 1, 256), num_sms() * 8));
-  k_pack_counts<<<g, 256, 0, s>>>(n, t->perm.p, d_p, d_diags, kind, t->rp.p, maxcnt.p);
+  if (n) {
+    k_pack_counts<<<g, 256, 0, s>>>(n, t->perm.p, d_p, d_diags, kind, t->len.p, hist.p);
+    check_launch();
+  }
+  int h_hist[kSlabMax + 2];
+  GB_CUDA(cudaMemcpyAsync(h_hist, hist.p, sizeof(h_hist), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  t->K = choose_slab_width(n, h_hist);
+  t->npad = std::max(n, 1);
+  t->ovp.alloc(n + 1);
+  k_overflow_counts<<<g, 256, 0, s>>>(n, t->len.p, t->K, t->ovp.p);
   check_launch();
   size_t tmp_bytes = 0;
-  GB_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, t->rp.p, t->rp.p, n + 1, s));
+  GB_CUDA(cub::DeviceScan::ExclusiveSum(nullptr, tmp_bytes, t->ovp.p, t->ovp.p, n + 1, s));
   DBuf<char> tmp(tmp_bytes);
-  GB_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, tmp_bytes, t->rp.p, t->rp.p, n + 1, s));
+  GB_CUDA(cub::DeviceScan::ExclusiveSum(tmp.p, tmp_bytes, t->ovp.p, t->ovp.p, n + 1, s));
   count_launch(2);
-  int nnz_off = 0;
-  GB_CUDA(cudaMemcpyAsync(&nnz_off, t->rp.p + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+  int nov = 0;
+  GB_CUDA(cudaMemcpyAsync(&nov, t->ovp.p + n, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
+  t->nov = nov;
+  long long nnz_off = 0;
+  for (int c = 0; c <= kSlabMax; ++c) nnz_off += (long long)c * h_hist[c];
+  t->sci.alloc((size_t)t->K * t->npad);
+  t->oci.alloc(nov);
+  if (vdtype == GBSYM_F64)
+    pack_values<double>(t.get(), d_p, d_i, d_x, d_diags, t->sv64, t->ov64, t->dg64, t->rc64, s);
+  else
+    pack_values<float>(t.get(), d_p, d_i, d_x, d_diags, t->sv32, t->ov32, t->dg32, t->rc32, s);
+  // exact off-diagonal count (rows longer than the histogram's last bin)
+  {
+    std::vector<int> lens(n);
+    if (n) GB_CUDA(cudaMemcpyAsync(lens.data(), t->len.p, n * sizeof(int), cudaMemcpyDeviceToHost, s));
+    GB_CUDA(cudaStreamSynchronize(s));
+    nnz_off = 0;
+    for (int v : lens) nnz_off += v;
+  }
   t->nnz_off = nnz_off;
-  t->ci.alloc(nnz_off);
-  const int gw = std::max(1, std::min(div_up(n, 8), num_sms() * 16));
-  if (vdtype == GBSYM_F64) {
-    t->val64.alloc(nnz_off);
-    t->dg64.alloc(n);
-    if (n)
-      k_pack_rows<double><<<gw, 256, 0, s>>>(n, t->perm.p, d_p, d_i, d_x, d_diags, kind, t->rp.p,
-                                             t->ci.p, t->val64.p, t->dg64.p);
-  } else {
-    t->val32.alloc(nnz_off);
-    t->dg32.alloc(n);
-    if (n)
-      k_pack_rows<float><<<gw, 256, 0, s>>>(n, t->perm.p, d_p, d_i, d_x, d_diags, kind, t->rp.p,
-                                            t->ci.p, t->val32.p, t->dg32.p);
-  }
-  if (n) check_launch();
-  // executor choice: one block when the whole solve is a short sweep
-  const char *force = std::getenv("GBSYM_TRI_EXEC");
-  t->exec = (t->max_level_rows <= 2048 && (double)n / std::max(1, t->nlev) <= 1024.0)
-                ? GBSYM_EXEC_ONEBLOCK
-                : GBSYM_EXEC_LEVELSET;
-  if (force) {
-    if (!std::strcmp(force, "levelset")) t->exec = GBSYM_EXEC_LEVELSET;
-    else if (!std::strcmp(force, "oneblock")) t->exec = GBSYM_EXEC_ONEBLOCK;
-  }
+  t->bar.alloc(1);
+  GB_CUDA(cudaMemsetAsync(t->bar.p, 0, sizeof(unsigned), s));
+  choose_exec(t.get());
   GB_CUDA(cudaStreamSynchronize(s));
   return t.release();
 }
@@ -838,15 +607,23 @@ extern "C" int gbsym_tri_get_info(gbsym_tri t, gbsym_tri_info *info) {
   info->exec = effective_exec(t, 1, false);
   info->max_level_rows = t->max_level_rows;
   const long long vs = t->vdtype == GBSYM_F64 ? 8 : 4;
-  info->bytes_matrix = t->nnz_off * (vs + 4) + (long long)t->n * (vs + 8) + 4 + (t->nlev + 1) * 4ll;
+  info->bytes_matrix = ((long long)t->K * t->npad + t->nov) * (vs + 4) + (long long)t->n * (2 * vs + 8) +
+                       (t->nov ? (t->n + 1) * 4ll : 0) + (t->nlev + 1) * 4ll;
   return GBSYM_OK;
 }
 
 extern "C" int gbsym_tri_set_exec(gbsym_tri t, int exec) {
   if (!t) return GBSYM_ERR_NULL_ARG;
-  if (exec < GBSYM_EXEC_AUTO || exec > GBSYM_EXEC_ONEBLOCK) return GBSYM_ERR_UNSUPPORTED;
+  if (exec < GBSYM_EXEC_AUTO || exec > GBSYM_EXEC_CLUSTER) return GBSYM_ERR_UNSUPPORTED;
   t->exec_forced = exec;
   return GBSYM_OK;
+}
+
+extern "C" int gbsym_tri_check(gbsym_tri t, void *stream) {
+  if (!t) return GBSYM_ERR_NULL_ARG;
+  int code = GBSYM_OK;
+  const int st = guarded([&] { code = tri_read_error(t, (cudaStream_t)stream); });
+  return st ? st : code;
 }
 
 extern "C" int gbsym_tri_get_schedule(gbsym_tri t, int *level_ptr, int *level_set) {
@@ -895,6 +672,7 @@ extern "C" int gbsym_tri_solve_host(gbsym_tri t, double *x, int k, int layout) {
     int st = gbsym_tri_solve(t, dx, k, layout, GBSYM_F64, s);
     if (st) throw Err{st};
     if (bytes) GB_CUDA(cudaMemcpyAsync(x, dx, bytes, cudaMemcpyDeviceToHost, s));
-    GB_CUDA(cudaStreamSynchronize(s));
+    const int code = tri_read_error(t, s);
+    if (code) throw Err{code};
   });
 }

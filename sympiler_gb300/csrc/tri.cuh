@@ -10,19 +10,34 @@
 
 namespace gbsym {
 
-// Device view of a level-packed triangle.  Packed row k is original row
-// perm[k]; its off-diagonal entries are ci/val[rp[k] .. rp[k+1]) in the
-// caller's storage order (column indices stay in the ORIGINAL numbering, so
-// x is addressed in the caller's order); dg[k] is its divisor, or dg is
-// null for a unit triangle.  Rows of level l occupy packed positions
-// lev_ptr[l] .. lev_ptr[l+1].
+// Device view of a level-packed triangle in sliced-ELL form.
+//
+// Packed row k is original row perm[k]; rows of level l occupy packed
+// positions lev_ptr[l] .. lev_ptr[l+1].  Row k has len[k] off-diagonal
+// entries, in the caller's storage order: the first min(len, K) of them
+// sit in a column-interleaved slab (entry q of row k at sci/sv[q*npad + k],
+// so a warp reading entry q of 32 consecutive rows reads one contiguous
+// run), the rest in an overflow CSR at ovp[k] (entry q >= K at
+// oci/ov[ovp[k] + q - K]).  Column indices keep the ORIGINAL numbering, so
+// x is addressed in the caller's order.  dg[k] is the row's divisor; dg is
+// null for a unit triangle; rc[k] = RN(1 / dg[k]).  Every static load of a row is independent of
+// the others (no row-pointer indirection for the slab), which is what lets
+// a level kernel finish them before it waits on the previous level.
+constexpr int kSlabMax = 8;
+
 template <class T>
 struct TriView {
+  int K;     // slab width, 0 .. kSlabMax
+  int npad;  // slab stride (>= n)
   const int *__restrict__ perm;
-  const int *__restrict__ rp;
-  const int *__restrict__ ci;
-  const T *__restrict__ val;
+  const int *__restrict__ len;
+  const int *__restrict__ sci;
+  const T *__restrict__ sv;
+  const int *__restrict__ ovp;  // null when no row overflows
+  const int *__restrict__ oci;
+  const T *__restrict__ ov;
   const T *__restrict__ dg;
+  const T *__restrict__ rc;  // RN(1/dg), for the exact Markstein division
 };
 
 // Internal kinds used only by the schedule builders: every stored entry on
@@ -54,13 +69,20 @@ struct gbsym_tri_s {
   int vdtype = GBSYM_F64;
   long long nnz_off = 0;
   int max_level_rows = 0;
-  int exec = GBSYM_EXEC_LEVELSET;  // autotuned
+  int exec = GBSYM_EXEC_LEVELSET;       // chosen executor for k = 1
+  int exec_mrhs = GBSYM_EXEC_LEVELSET;  // chosen executor for k > 1
   int exec_forced = GBSYM_EXEC_AUTO;
+  int persist_blocks = 0;               // cap on the persistent grid (0: none)
+  int cluster_blocks = 0;               // cap on blocks per cluster (0: none)
   std::vector<int> h_lev_ptr;        // packed level boundaries (host copy)
-  gbsym::DBuf<int> lev_ptr, perm, rp, ci;
-  gbsym::DBuf<double> val64, dg64;
-  gbsym::DBuf<float> val32, dg32;
-  gbsym::DBuf<int> err;              // device error word(s)
+  int K = 0, npad = 0;               // slab width and stride
+  long long nov = 0;                 // overflow entries
+  gbsym::DBuf<int> lev_ptr, perm, len, sci, ovp, oci;
+  gbsym::DBuf<double> sv64, ov64, dg64, rc64;
+  gbsym::DBuf<float> sv32, ov32, dg32, rc32;
+  int arith = GBSYM_ARITH_EXACT;      // GBSYM_ARITH_EXACT or GBSYM_ARITH_FUSED
+  gbsym::DBuf<int> err;              // device error word(s): code, where
+  gbsym::DBuf<unsigned> bar;         // grid-barrier arrival counter
   gbsym::DBuf<int> flags;            // sync-free ready flags (per packed row)
   gbsym::DBuf<int> ticket;           // sync-free work counter
   int epoch = 0;                     // sync-free flag generation
@@ -71,10 +93,12 @@ struct gbsym_tri_s {
   unsigned long long graph_clock = 0;
 
   gbsym::TriView<double> view64() const {
-    return {perm.p, rp.p, ci.p, val64.p, kind == GBSYM_ILU_UNIT_LOWER ? nullptr : dg64.p};
+    return {K, npad, perm.p, len.p, sci.p, sv64.p, nov ? ovp.p : nullptr, oci.p, ov64.p,
+            kind == GBSYM_ILU_UNIT_LOWER ? nullptr : dg64.p, rc64.p};
   }
   gbsym::TriView<float> view32() const {
-    return {perm.p, rp.p, ci.p, val32.p, kind == GBSYM_ILU_UNIT_LOWER ? nullptr : dg32.p};
+    return {K, npad, perm.p, len.p, sci.p, sv32.p, nov ? ovp.p : nullptr, oci.p, ov32.p,
+            kind == GBSYM_ILU_UNIT_LOWER ? nullptr : dg32.p, rc32.p};
   }
   ~gbsym_tri_s();
 };
@@ -84,6 +108,11 @@ namespace gbsym {
 // selects the "redundant" row formula (k == 1, FP64 only).
 void tri_solve_rowmajor(gbsym_tri_s *t, void *x, const void *b, int k, int dtype,
                         cudaStream_t s);
+// Executor selection (exec.cu).
+void choose_exec(gbsym_tri_s *t);
+int effective_exec(const gbsym_tri_s *t, int k, bool redundant);
+// Synchronises s and returns (and clears) the plan's sticky device error.
+int tri_read_error(gbsym_tri_s *t, cudaStream_t s);
 // Build a plan from device arrays (validates matrix and schedule).
 gbsym_tri_s *tri_build(int n, const int *d_p, const int *d_i, const double *d_x,
                        const int *d_diags, int kind, int vdtype,

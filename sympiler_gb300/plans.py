@@ -118,6 +118,21 @@ class TriPlan:
     def set_exec(self, exec_mode: int):
         check(lib().gbsym_tri_set_exec(self._h, int(exec_mode)), "gbsym_tri_set_exec")
 
+    def set_arith(self, arith: int):
+        check(lib().gbsym_tri_set_arith(self._h, int(arith)), "gbsym_tri_set_arith")
+
+    def autotune(self, k=1, dtype=None, stream=None) -> int:
+        """Time every executor for k right-hand sides; returns the chosen one."""
+        chosen = C.c_int(0)
+        dt = self.dtype if dtype is None else _dtype_code(dtype)
+        check(lib().gbsym_tri_autotune(self._h, int(k), dt, _stream(stream), C.byref(chosen)),
+              "gbsym_tri_autotune")
+        return chosen.value
+
+    def check(self, stream=None):
+        """Wait for the stream; raise if a device-side check recorded an error."""
+        check(lib().gbsym_tri_check(self._h, _stream(stream)), "gbsym_tri_check")
+
     def solve(self, x, layout=L.ROW_MAJOR, stream=None):
         """In place on a CUDA tensor of shape (n,) or (n, k) row-major
         (or (k, n) with layout=COL_MAJOR, i.e. column-major n x k)."""
