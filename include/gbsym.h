@@ -229,6 +229,11 @@ int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, int *chosen)
  * this plan recorded since the last call (e.g. GBSYM_ERR_TIMEOUT from a
  * bounded wait), clearing it; GBSYM_OK when none. */
 int gbsym_tri_check(gbsym_tri t, void *stream);
+/* Failure-detection self-test: runs the executors' bounded grid-barrier
+ * wait with one participant that never arrives and a limit of limit_ns
+ * (at most 10 s).  Returns GBSYM_ERR_TIMEOUT when the wait gave up and
+ * reported it, which is the expected outcome; the context stays usable. */
+int gbsym_selftest_bounded_wait(long long limit_ns, void *stream);
 /* Copy the schedule into host buffers of levels+1 and n ints. */
 int gbsym_tri_get_schedule(gbsym_tri t, int *level_ptr, int *level_set);
 

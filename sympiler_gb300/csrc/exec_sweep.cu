@@ -17,7 +17,8 @@ namespace gbsym {
 // stores, then polls with acquire until all blocks of generation `target`
 // have arrived.  Returns false (and records GBSYM_ERR_TIMEOUT) when the
 // wait runs out, after which every block leaves the sweep.
-__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target, int *err) {
+__device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target, int *err,
+                                             unsigned long long limit_ns = kWaitLimitNs) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -28,7 +29,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned *bar, unsigned target, int
     const unsigned long long t0 = globaltimer_ns();
     while ((int)(ld_acquire_u32(bar) - target) < 0) {
       ++it;
-      if (it > kWaitLimitIters || ((it & 255) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) ||
+      if (it > kWaitLimitIters || ((it & 255) == 0 && globaltimer_ns() - t0 > limit_ns) ||
           ((it & 255) == 0 && ld_relaxed(err) != 0)) {
         atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
         ok = 0;
@@ -205,9 +206,39 @@ void run_persist(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
   else persist_ar<T, kArithExact>(t, x, k, s);
 }
 
+// Self-test of the bounded wait: block 1 never arrives, so block 0's barrier
+// wait can only end through its limit, recording GBSYM_ERR_TIMEOUT.
+__global__ void k_selftest_barrier(unsigned *bar, int *err, unsigned long long limit_ns) {
+  if (blockIdx.x == 1) return;
+  grid_barrier(bar, 2u, err, limit_ns);
+}
+
+int selftest_timeout(unsigned long long limit_ns, cudaStream_t s) {
+  DBuf<unsigned> bar(1);
+  DBuf<int> err(2);
+  GB_CUDA(cudaMemsetAsync(bar.p, 0, sizeof(unsigned), s));
+  GB_CUDA(cudaMemsetAsync(err.p, 0, 2 * sizeof(int), s));
+  unsigned *bp = bar.p;
+  int *ep = err.p;
+  void *params[] = {(void *)&bp, (void *)&ep, (void *)&limit_ns};
+  GB_CUDA(cudaLaunchCooperativeKernel((const void *)k_selftest_barrier, dim3(2), dim3(32), params, 0, s));
+  check_launch();
+  int h[2];
+  GB_CUDA(cudaMemcpyAsync(h, err.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  return h[0];
+}
+
 template void run_oneblock<double>(gbsym_tri_s *, double *, cudaStream_t);
 template void run_oneblock<float>(gbsym_tri_s *, float *, cudaStream_t);
 template void run_persist<double>(gbsym_tri_s *, double *, int, cudaStream_t);
 template void run_persist<float>(gbsym_tri_s *, float *, int, cudaStream_t);
 
 }  // namespace gbsym
+
+extern "C" int gbsym_selftest_bounded_wait(long long limit_ns, void *stream) {
+  if (limit_ns <= 0 || limit_ns > 10000000000ll) return GBSYM_ERR_SIZE;
+  int code = GBSYM_OK;
+  const int st = gbsym::guarded([&] { code = gbsym::selftest_timeout((unsigned long long)limit_ns, (cudaStream_t)stream); });
+  return st ? st : code;
+}

@@ -83,9 +83,13 @@ struct gbsym_tri_s {
   int arith = GBSYM_ARITH_EXACT;      // GBSYM_ARITH_EXACT or GBSYM_ARITH_FUSED
   gbsym::DBuf<int> err;              // device error word(s): code, where
   gbsym::DBuf<unsigned> bar;         // grid-barrier arrival counter
-  gbsym::DBuf<int> flags;            // sync-free ready flags (per packed row)
-  gbsym::DBuf<int> ticket;           // sync-free work counter
-  int epoch = 0;                     // sync-free flag generation
+  gbsym::DBuf<char> sfy;             // sync-free published values (sentinel-filled)
+  struct SfUnits {
+    int rpw = 0, n = 0;
+    gbsym::DBuf<int> row, cnt;       // level-aligned warp units
+  };
+  std::vector<SfUnits> sf_units;
+  int sf_blocks_per_sm = 0;          // sync-free grid (0: default)
   gbsym::DBuf<char> scratch;         // layout-conversion scratch
   gbsym::DBuf<char> io;              // device copy for host-memory solves
   cudaStream_t cap_stream = nullptr; // private stream for graph capture
