@@ -319,6 +319,22 @@ int gbsym_batch_destroy(gbsym_batch b);
 int gbsym_batch_solve(gbsym_batch b, void *x, int k, int dtype, void *stream);
 int gbsym_batch_row_offsets(gbsym_batch b, long long *offsets);
 
+/* ---- forward solve that allocates nothing ------------------------------ */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- an application whose own pool allocator owns all device memory,
+ * or a loop that cannot take the device-wide synchronisation of cudaMalloc/
+ * cudaFree.  Solves L x = b in place (x holds b on entry), L lower CSR with
+ * the diagonal last in each row, all pointers DEVICE pointers, with the
+ * reference sptrsv_csr arithmetic (bit-identical results).  Its only scratch
+ * is a static device array inside this library (4 MiB per GPU, held until
+ * the process exits), so n is limited to 524,288 rows; larger n returns
+ * GBSYM_ERR_SIZE without touching x.  The first call on a device looks up
+ * that array's address and should come before any stream capture; calls
+ * that overlap on the GPU share the array and race.  Returns when the
+ * solve is done (synchronises `stream`). */
+int gbsym_sptrsv_csr_noalloc(int n, const int *Lp, const int *Li, const double *Lx, double *x,
+                             void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -84,6 +84,7 @@ SIGNATURES = {
     "gbsym_batch_destroy": (_int, [_vp]),
     "gbsym_batch_solve": (_int, [_vp, _vp, _int, _int, _vp]),
     "gbsym_batch_row_offsets": (_int, [_vp, _vp]),
+    "gbsym_sptrsv_csr_noalloc": (_int, [_int, _vp, _vp, _vp, _vp, _vp]),
 }
 
 _lib = None
