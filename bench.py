@@ -59,6 +59,18 @@ def algorithmic_bytes(nnz_l, n, k, vbytes=8, sbytes=8):
     return (vbytes + 4) * nnz_l + 4 * (n + 1) + 2 * sbytes * k * n
 
 
+# FP64 throughput of this machine's GB300 (dependent-free DFMA stream, all SMs):
+# 502 G operations/s, measured by a microbenchmark during development.  On
+# this part the FP64 pipe, not HBM, bounds an FP64 triangular solve.
+FP64_PEAK_GOPS = 502.0
+
+
+def fp64_ops_exact(nnz_off, n, k):
+    """FP64 operations of one exact solve: a multiply and a subtract per
+    stored off-diagonal, three for the correctly rounded division."""
+    return k * (2 * nnz_off + 3 * n)
+
+
 def config(grid, k):
     return {"workload": "C2 IC0 factor of 3D 7-pt Laplacian %d^3 + 1e-2 I, forward SpTRSV, %d RHS FP64"
                         % (grid, k),
@@ -212,6 +224,104 @@ def cpu_baseline_sample(L, k, nl, lp, ls):
                       "reps, scaled to %d RHS" % (cores, cols, reps, k)}
 
 
+def _time(fn, reps, stream, flush=None):
+    import torch
+    ts = []
+    for _ in range(reps):
+        if flush is not None:
+            flush.fill_(7)
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        fn()
+        b.record(stream)
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b) / 1e3)
+    return statistics.median(ts)
+
+
+def bench_batch(dev, stream, flush, nsys=512, k=8):
+    """512 uneven SPD systems (80% shifted 2D Laplacians on 30..300 grids,
+    20% random diagonally dominant, n 900..90,000), IC0 on the GPU, all
+    systems solved in one executor pass with 8 right-hand sides."""
+    import torch
+    from sympiler_gb300 import matgen as mg
+    from sympiler_gb300 import plans
+    from sympiler_gb300._lib import LOWER_CSC
+    t0 = time.perf_counter()
+    systems = mg.batch_systems_upper(nsys, np.random.default_rng(44))
+    N, up, ui, ux, off = mg.block_diagonal(systems)
+    dp, di = torch.from_numpy(up).to(dev), torch.from_numpy(ui).to(dev)
+    dv = torch.from_numpy(ux).to(dev)
+    plans.ic0_device(N, dv, dp, di)          # IC0 of every system at once
+    res = {"systems": nsys, "rows": N, "nnz_L": int(up[-1]), "setup_s": None}
+    rng = np.random.default_rng(45)
+    for dt in ("f64", "f32"):
+        P = plans.TriPlan(N, dp, di, dv, kind=LOWER_CSC, dtype=dt)
+        tdt = torch.float64 if dt == "f64" else torch.float32
+        B = torch.from_numpy(rng.standard_normal((N, k))).to(dev).to(tdt)
+        X = torch.empty_like(B)
+        chosen = P.autotune(k=k, dtype=dt)
+        info = P.info()
+
+        def run():
+            X.copy_(B)
+            P.solve(X)
+        run()
+        t = _time(run, 5, stream, flush)
+        vb, sb = (8, 8) if dt == "f64" else (4, 4)
+        byt = algorithmic_bytes(int(info.nnz_off) + N, N, k, vb, sb)
+        res[dt] = {"ms": t * 1e3, "batch_solves_per_s": 1.0 / t, "gbs": byt / t / 1e9,
+                   "levels": info.levels, "executor": chosen}
+        del P, B, X
+    res["setup_s"] = time.perf_counter() - t0
+    return res
+
+
+def bench_adjoint(dev, stream, flush, g=1024, k=32):
+    """Forward X = L^{-1} B and the reverse pass (L^T solve + value gradient)
+    on the IC0 factor of the 1024^2 anisotropic variable-coefficient Poisson
+    operator, 32 right-hand sides, FP64."""
+    import torch
+    from sympiler_gb300 import matgen as mg
+    from sympiler_gb300 import plans
+    from sympiler_gb300._lib import LOWER_CSC, UPPER_DIAG_FIRST
+    rng = np.random.default_rng(55)
+    A = mg.aniso_poisson2d(g, 0.01, 1.0, rng)
+    U = mg.triu(A)
+    dp, di = torch.from_numpy(U.p).to(dev), torch.from_numpy(U.i).to(dev)
+    dv = torch.from_numpy(U.x.copy()).to(dev)
+    plans.ic0_device(U.n, dv, dp, di)
+    Lf = plans.TriPlan(U.n, dp, di, dv, kind=LOWER_CSC)
+    Lt = plans.TriPlan(U.n, dp, di, dv, kind=UPPER_DIAG_FIRST)
+    Lcsr = mg.transpose(mg.CSR(U.n, U.p, U.i, dv.cpu().numpy()))
+    lp, li = torch.from_numpy(Lcsr.p).to(dev), torch.from_numpy(Lcsr.i).to(dev)
+    ef = Lf.autotune(k=k)
+    et = Lt.autotune(k=k)
+    B = torch.from_numpy(rng.standard_normal((U.n, k))).to(dev)
+    W = torch.from_numpy(rng.standard_normal((U.n, k))).to(dev)
+    X = torch.empty_like(B)
+    G = torch.empty_like(W)
+    grad = torch.empty(Lcsr.nnz, dtype=torch.float64, device=dev)
+
+    def fwd():
+        X.copy_(B)
+        Lf.solve(X)
+
+    def bwd():
+        G.copy_(W)
+        plans.tri_adjoint(Lt, U.n, lp, li, X, G, grad)
+    fwd()
+    bwd()
+    tf = _time(fwd, 5, stream, flush)
+    tb = _time(bwd, 5, stream, flush)
+    info = Lf.info()
+    byt = algorithmic_bytes(Lcsr.nnz, U.n, k)
+    return {"n": U.n, "nnz_L": Lcsr.nnz, "levels": info.levels, "rhs": k,
+            "forward_ms": tf * 1e3, "forward_gbs": byt / tf / 1e9, "backward_ms": tb * 1e3,
+            "executors": {"forward": ef, "transposed": et}}
+
+
 def load_traffic(workload_key):
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -348,6 +458,11 @@ def main():
                          "algorithmic_bytes_per_solve": byt,
                          "note": "one launch = one forward solve (graph of per-level kernels); "
                                  "duration from CUDA events on the launch stream"},
+            "roofline_fp64": {"bound": "fp64 pipe", "achieved": fp64_ops_exact(int(info.nnz_off), n, k) / t_step / 1e9,
+                              "peak": FP64_PEAK_GOPS, "unit": "G FP64 op/s",
+                              "frac": fp64_ops_exact(int(info.nnz_off), n, k) / t_step / 1e9 / FP64_PEAK_GOPS,
+                              "ops_per_solve": fp64_ops_exact(int(info.nnz_off), n, k),
+                              "peak_source": "measured (DFMA throughput microbenchmark, this pool)"},
             "e2e": {"value": byt / e2e_step / 1e9, "unit": UNIT, "h2d_bytes_per_step": n * k * 8,
                     "d2h_bytes_per_step": n * k * 8, "ms_per_step": e2e_step * 1e3,
                     "api": "gbsym_tri_solve_host (pinned host x, row-major)"},
@@ -448,6 +563,9 @@ def main():
                          "relres": best.relres, "status": best.status}
         out["speedup_fp32_precond"] = out["f64"]["seconds"] / out["f32"]["seconds"]
         extras["gmres_c3"] = out
+        del Cp, dC, lu
+        extras["batch_c4"] = bench_batch(dev, stream, flush)
+        extras["adjoint_c5"] = bench_adjoint(dev, stream, flush)
         result["extras"] = extras
     if rank == 0:
         if not args.extras_only:

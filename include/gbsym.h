@@ -167,7 +167,9 @@ enum gbsym_tri_kind {
                                  the CSR of an upper triangle              */
   GBSYM_ILU_UNIT_LOWER = 2,   /* [p[i], diags[i]), no division            */
   GBSYM_ILU_UPPER = 3,        /* (diags[i], p[i+1]), divide by diagonal   */
-  GBSYM_ILU_LOWER_DIV = 4     /* [p[i], diags[i]), divide by l[diags[i]]  */
+  GBSYM_ILU_LOWER_DIV = 4,    /* [p[i], diags[i]), divide by l[diags[i]]  */
+  GBSYM_LOWER_CSC = 5         /* CSC of L, diagonal first in each column
+                                 (sptrsv_csc); transposed on the GPU      */
 };
 enum gbsym_dtype { GBSYM_F64 = 0, GBSYM_F32 = 1 };
 enum gbsym_layout { GBSYM_COL_MAJOR = 0, GBSYM_ROW_MAJOR = 1 };

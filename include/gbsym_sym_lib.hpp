@@ -1,0 +1,135 @@
+// gbsym_sym_lib.hpp -- drop-in for the triangular-solve path of the
+// reference's C++ API (include/sympiler/sparse_blas_lib.h, namespace
+// sym_lib; include/sympiler/parsy/triangularSolve/Triangular_CSC.h and
+// include/sympiler/parsy/gmres/mgmres.hpp, namespace sym_lib::parsy).
+//
+// A caller that included those headers includes this one instead and links
+// libgbsym.so in place of the reference's sparse_blas objects: the
+// signatures, argument meanings and in-place behaviour are the reference's,
+// the work runs on the GPU.  The void functions never abort; their status
+// is available from gbsym_last_error().
+//
+// build_levelSet_CSC stands in for the reference's (unvendored) aggregation
+// dependency at its call sites (Catch_tests/sptrsv_tests.cpp:59,
+// demo/sptrsv_demo_utils.h:42-45): it returns arrays allocated with new[],
+// which those callers release with delete[].
+#ifndef GBSYM_SYM_LIB_HPP
+#define GBSYM_SYM_LIB_HPP
+
+#include <cstddef>
+#include <cstring>
+
+#include "gbsym.h"
+
+namespace sym_lib {
+
+// ---- SpMV (sparse_blas_lib.h:19-37) ----------------------------------------
+inline void spmv_csr(int n, const int *Ap, const int *Ai, const double *Ax, const double *x,
+                     double *y) {
+  gbsym_spmv_csr(n, Ap, Ai, Ax, x, y);
+}
+inline void spmv_csr(int n, const int *Ap, const int *Ai, const double *Ax, const double *x,
+                     const double *y, double *z, double a, double b) {
+  gbsym_spmv_csr_axpby(n, Ap, Ai, Ax, x, y, z, a, b);
+}
+inline void spmv_csr_parallel(int n, const int *Ap, const int *Ai, const double *Ax,
+                              const double *x, double *y) {
+  gbsym_spmv_csr_parallel(n, Ap, Ai, Ax, x, y);
+}
+
+// ---- SpTRSV, CSR (sparse_blas_lib.h:126-161) ---------------------------------
+inline void sptrsv_csr(int n, int *Lp, int *Li, double *Lx, double *x) {
+  gbsym_sptrsv_csr(n, Lp, Li, Lx, x);
+}
+inline void sptrsv_csr_ilu(int n, const int *Lp, const int *Li, const double *Lx,
+                           const int *diags, double *x) {
+  gbsym_sptrsv_csr_ilu(n, Lp, Li, Lx, diags, x);
+}
+inline void sptrsv_csr_ilu_lbc(int n, const int *Lp, const int *Li, const double *Lx,
+                               const int *diags, double *x, const int level_no,
+                               const int *level_ptr, const int *par_ptr, const int *partition) {
+  gbsym_sptrsv_csr_ilu_lbc(n, Lp, Li, Lx, diags, x, level_no, level_ptr, par_ptr, partition);
+}
+inline void sptrsv_csr_levelset(int n, const int *Lp, const int *Li, const double *Lx, double *x,
+                                int levels, const int *levelPtr, const int *levelSet) {
+  gbsym_sptrsv_csr_levelset(n, Lp, Li, Lx, x, levels, levelPtr, levelSet);
+}
+inline void sptrsv_csr_lbc(int n, int *Lp, int *Li, double *Lx, double *x, int level_no,
+                           int *level_ptr, int *par_ptr, int *partition) {
+  gbsym_sptrsv_csr_lbc(n, Lp, Li, Lx, x, level_no, level_ptr, par_ptr, partition);
+}
+inline void sptrsv_csr_lbc_redundant(int n, int *Lp, int *Li, double *Lx, double *x, double *b,
+                                     int level_no, int *level_ptr, int *par_ptr, int *partition,
+                                     double *tmp) {
+  gbsym_sptrsv_csr_lbc_redundant(n, Lp, Li, Lx, x, b, level_no, level_ptr, par_ptr, partition, tmp);
+}
+
+// ---- SpTRSV, CSC (sparse_blas_lib.h:170-178, 330) ------------------------------
+inline void sptrsv_csc(int n, int *Lp, int *Li, double *Lx, double *x) {
+  gbsym_sptrsv_csc(n, Lp, Li, Lx, x);
+}
+inline void sptrsv_csc_levelset(int n, int *Lp, int *Li, double *Lx, double *x, int levels,
+                                const int *levelptr, const int *levelset) {
+  gbsym_sptrsv_csc_levelset(n, Lp, Li, Lx, x, levels, levelptr, levelset);
+}
+inline void sptrsv_csc_lbc(int n, int *Lp, int *Li, double *Lx, double *x, int level_no,
+                           int *level_ptr, int *par_ptr, int *partition) {
+  gbsym_sptrsv_csc_lbc(n, Lp, Li, Lx, x, level_no, level_ptr, par_ptr, partition);
+}
+inline int ltsolve(int n, int *Lp, int *Li, double *Lx, double *x) {
+  return gbsym_ltsolve(n, Lp, Li, Lx, x);
+}
+
+// ---- factor producers (sparse_blas_lib.h:242, 276-277) ---------------------------
+inline void spic0_csr(int n, double *val, int *rowPtr, int *rowIdx) {
+  gbsym_spic0_csr(n, val, rowPtr, rowIdx);
+}
+inline void spilu0_csr(int n, int nnz, const int *Ap, const int *Ai, const double *Ax,
+                       const int *A_diag, double *l) {
+  gbsym_spilu0_csr(n, nnz, Ap, Ai, Ax, A_diag, l);
+}
+
+// ---- schedule builder at the reference's build_levelSet_CSC call sites ------------
+inline int build_levelSet_CSC(size_t n, const int *Lp, const int *Li, int *&levelPtr,
+                              int *&levelSet) {
+  int *lp = nullptr, *ls = nullptr;
+  const int nl = gbsym_build_levelset_csc((int)n, Lp, Li, &lp, &ls);
+  levelPtr = nullptr;
+  levelSet = nullptr;
+  if (nl < 0) return nl;
+  levelPtr = new int[nl + 1];
+  levelSet = new int[n > 0 ? n : 1];
+  std::memcpy(levelPtr, lp, sizeof(int) * (size_t)(nl + 1));
+  if (n) std::memcpy(levelSet, ls, sizeof(int) * n);
+  gbsym_free(lp);
+  gbsym_free(ls);
+  return nl;
+}
+
+namespace parsy {
+// Triangular_CSC.h:14-36
+inline int lsolve(int n, int *Lp, int *Li, double *Lx, double *x) {
+  return gbsym_parsy_lsolve(n, Lp, Li, Lx, x);
+}
+inline int ltsolve(int n, int *Lp, int *Li, double *Lx, double *x) {
+  return gbsym_parsy_ltsolve(n, Lp, Li, Lx, x);
+}
+inline int lsolvePar(int n, int *Lp, int *Li, double *Lx, double *x, int levels, int *levelPtr,
+                     int *levelSet, int chunk) {
+  return gbsym_parsy_lsolvePar(n, Lp, Li, Lx, x, levels, levelPtr, levelSet, chunk);
+}
+inline int lsolveParH2(int n, int *Lp, int *Li, double *Lx, double *x, int levels, int *levelPtr,
+                       int *levelSet, int parts, int *parPtr, int *partition, int chunk) {
+  return gbsym_parsy_lsolveParH2(n, Lp, Li, Lx, x, levels, levelPtr, levelSet, parts, parPtr,
+                                 partition, chunk);
+}
+// mgmres.hpp:41
+inline void lus_cr(int n, int nz_num, int ia[], int ja[], double l[], int ua[], double r[],
+                   double z[]) {
+  gbsym_parsy_lus_cr(n, nz_num, ia, ja, l, ua, r, z);
+}
+}  // namespace parsy
+
+}  // namespace sym_lib
+
+#endif

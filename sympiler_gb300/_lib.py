@@ -117,7 +117,7 @@ class GbsymError(RuntimeError):
 # status codes (include/gbsym.h)
 OK, ERR_NULL_ARG, ERR_BAD_SCHEDULE, ERR_PIVOT, ERR_TIMEOUT, ERR_CUDA, ERR_BAD_MATRIX, ERR_SIZE, \
     ERR_NOT_CONVERGED, ERR_UNSUPPORTED = range(10)
-LOWER_DIAG_LAST, UPPER_DIAG_FIRST, ILU_UNIT_LOWER, ILU_UPPER, ILU_LOWER_DIV = range(5)
+LOWER_DIAG_LAST, UPPER_DIAG_FIRST, ILU_UNIT_LOWER, ILU_UPPER, ILU_LOWER_DIV, LOWER_CSC = range(6)
 F64, F32 = 0, 1
 COL_MAJOR, ROW_MAJOR = 0, 1
 EXEC_AUTO, EXEC_LEVELSET, EXEC_SYNCFREE, EXEC_ONEBLOCK, EXEC_PERSISTENT, EXEC_CLUSTER = range(6)

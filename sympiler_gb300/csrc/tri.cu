@@ -529,6 +529,45 @@ gbsym_tri_s::~gbsym_tri_s() {
   if (cap_stream) cudaStreamDestroy(cap_stream);
 }
 
+namespace gbsym {
+
+// ---------------------------------------------------------------------------
+// CSC input: every column starts with its diagonal and lists rows below it
+__global__ void k_check_csc_lower(int n, const int *__restrict__ p, const int *__restrict__ ri, int *err) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int a = p[j], z = p[j + 1];
+    bool bad = z <= a || ri[a] != j;
+    for (int e = a + 1; !bad && e < z; ++e) bad = ri[e] <= j || ri[e] >= n;
+    if (bad) record_error(err, GBSYM_ERR_BAD_MATRIX, j);
+  }
+}
+
+void check_csc_lower(int n, const int *p, const int *ri, cudaStream_t s) {
+  if (!n) return;
+  DBuf<int> err(2);
+  GB_CUDA(cudaMemsetAsync(err.p, 0, 2 * sizeof(int), s));
+  k_check_csc_lower<<<std::min(div_up(n, 256), num_sms() * 8), 256, 0, s>>>(n, p, ri, err.p);
+  check_launch();
+  int h[2];
+  read_err(err, s, h);
+  if (h[0]) throw Err{h[0]};
+}
+
+__global__ void k_gather_f64(long long m, const double *__restrict__ src, const int *__restrict__ idx,
+                             double *dst) {
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < m;
+       t += (long long)gridDim.x * blockDim.x)
+    dst[t] = src[idx[t]];
+}
+
+void gather_values(long long m, const double *src, const int *idx, double *dst, cudaStream_t s) {
+  if (!m) return;
+  k_gather_f64<<<(int)std::min<long long>(div_up(m, 256), num_sms() * 8), 256, 0, s>>>(m, src, idx, dst);
+  check_launch();
+}
+
+}  // namespace gbsym
+
 // ---------------------------------------------------------------------------
 // C API: plans
 using namespace gbsym;
@@ -587,6 +626,25 @@ extern "C" int gbsym_tri_create(gbsym_tri *out, int n, const int *p, const int *
       GB_CUDA(cudaMemcpyAsync(hlp.data(), level_ptr, (levels + 1) * sizeof(int),
                               cudaMemcpyDeviceToHost, s));
       GB_CUDA(cudaStreamSynchronize(s));
+    }
+    if (kind == GBSYM_LOWER_CSC) {
+      // CSC of a lower triangle (diagonal first in each column): transpose
+      // on the device into the CSR pull form (diagonal last in each row).
+      // The transposed rows list columns ascending, the order in which the
+      // column-push solve (sptrsv_csc) updates each row.
+      int nz = 0;
+      if (n) {
+        GB_CUDA(cudaMemcpyAsync(&nz, pp + n, sizeof(int), cudaMemcpyDeviceToHost, s));
+        GB_CUDA(cudaStreamSynchronize(s));
+      }
+      check_csc_lower(n, pp, ii, s);
+      Transposed T;
+      transpose_pattern(n, nz, pp, ii, T, s);
+      DBuf<double> tx(nz);
+      gather_values(nz, xx, T.src.p, tx.p, s);
+      *out = tri_build(n, T.rp.p, T.ci.p, tx.p, nullptr, GBSYM_LOWER_DIAG_LAST, value_dtype,
+                       level_set ? hlp.data() : nullptr, ls, levels, s);
+      return;
     }
     *out = tri_build(n, pp, ii, xx, dg, kind, value_dtype, level_set ? hlp.data() : nullptr, ls,
                      levels, s);

@@ -217,3 +217,74 @@ def levels_wavefront(a: CSR) -> int:
             m = max(m, lev[i[j]])
         lev[r] = m + 1
     return int(lev.max() + 1) if a.n else 0
+
+
+# ---- batched workload ----------------------------------------------------
+
+def _lap2d_upper_shifted(nx: int, ny: int, shift: float):
+    """Upper CSR (diagonal first) of the 5-point Laplacian + shift*I."""
+    n = nx * ny
+    idx = np.arange(n)
+    x = idx % nx
+    y = idx // nx
+    right = x < nx - 1
+    up = y < ny - 1
+    cnt = 1 + right.astype(np.int64) + up.astype(np.int64)
+    p = np.zeros(n + 1, dtype=np.int64)
+    np.cumsum(cnt, out=p[1:])
+    nnz = int(p[-1])
+    ci = np.empty(nnz, dtype=np.int32)
+    cv = np.empty(nnz, dtype=np.float64)
+    ci[p[:-1]] = idx
+    cv[p[:-1]] = 4.0 + shift
+    pos = p[:-1] + 1
+    ci[pos[right]] = idx[right] + 1
+    cv[pos[right]] = -1.0
+    pos2 = pos + right
+    ci[pos2[up]] = idx[up] + nx
+    cv[pos2[up]] = -1.0
+    return n, p.astype(np.int32), ci, cv
+
+
+def batch_systems_upper(nsys: int = 512, rng: np.random.Generator | None = None,
+                        lap_frac: float = 0.8, grid=(30, 300), rand_n=(900, 90000)):
+    """The batched-solve workload: nsys independent SPD systems, as upper CSRs
+    (diagonal first; the CSC of their lower triangles).  A fraction lap_frac
+    are 2D 5-point Laplacians on nx, ny ~ U{grid} with a diagonal shift
+    ~ U[1e-3, 1]; the rest are random symmetric matrices with about 8
+    entries per row and N(0,1) off-diagonals, made strictly diagonally
+    dominant, with n ~ U{rand_n}.  Returns a list of (n, p, i, x)."""
+    rng = np.random.default_rng(0) if rng is None else rng
+    out = []
+    for q in range(nsys):
+        if rng.uniform() < lap_frac:
+            nx, ny = (int(v) for v in rng.integers(grid[0], grid[1] + 1, size=2))
+            out.append(_lap2d_upper_shifted(nx, ny, float(rng.uniform(1e-3, 1.0))))
+        else:
+            n = int(rng.integers(rand_n[0], rand_n[1] + 1))
+            U = triu(random_spd(n, 8, rng))
+            out.append((U.n, U.p, U.i, U.x))
+    return out
+
+
+def block_diagonal(systems):
+    """Concatenate square CSRs into one block-diagonal CSR; returns
+    (N, p, i, x, row_offsets)."""
+    ns = [s[0] for s in systems]
+    off = np.zeros(len(systems) + 1, dtype=np.int64)
+    np.cumsum(ns, out=off[1:])
+    nnzs = [int(s[1][-1]) for s in systems]
+    eoff = np.zeros(len(systems) + 1, dtype=np.int64)
+    np.cumsum(nnzs, out=eoff[1:])
+    N, E = int(off[-1]), int(eoff[-1])
+    if N >= 2 ** 31 or E >= 2 ** 31:
+        raise ValueError("batch too large for int32 indices")
+    p = np.empty(N + 1, dtype=np.int32)
+    ci = np.empty(E, dtype=np.int32)
+    cx = np.empty(E, dtype=np.float64)
+    for q, (n, sp_, si, sx) in enumerate(systems):
+        p[off[q]:off[q + 1]] = sp_[:-1] + eoff[q]
+        ci[eoff[q]:eoff[q + 1]] = si + off[q]
+        cx[eoff[q]:eoff[q + 1]] = sx
+    p[N] = E
+    return N, p, ci, cx, off

@@ -42,3 +42,43 @@ def test_status_strings_without_gpu():
     assert L.gbsym_status_string(0) == b"ok"
     assert b"schedule" in L.gbsym_status_string(_lib.ERR_BAD_SCHEDULE)
     assert L.gbsym_last_error() == 0
+
+
+def test_cpp_shim_compiles_and_links(tmp_path):
+    """A caller written against the reference's sym_lib signatures compiles
+    against include/gbsym_sym_lib.hpp and links libgbsym.so (nothing is run:
+    no GPU here)."""
+    from sympiler_gb300 import _lib
+    src = tmp_path / "caller.cpp"
+    src.write_text(r'''
+#include "gbsym_sym_lib.hpp"
+#include <cstdio>
+int main(int argc, char **argv) {
+  if (argc > 99) {  // never taken: only the symbols and signatures matter here
+    int n = 1, p[2] = {0, 1}, i[1] = {0}, *lp = nullptr, *ls = nullptr;
+    double v[1] = {1.0}, x[1] = {1.0}, y[1] = {0.0}, z[1] = {0.0};
+    sym_lib::sptrsv_csr(n, p, i, v, x);
+    sym_lib::sptrsv_csr_levelset(n, p, i, v, x, 1, p, i);
+    sym_lib::sptrsv_csr_lbc(n, p, i, v, x, 1, p, p, i);
+    sym_lib::sptrsv_csr_ilu(n, p, i, v, i, x);
+    sym_lib::sptrsv_csc(n, p, i, v, x);
+    sym_lib::spmv_csr(n, p, i, v, x, y);
+    sym_lib::spmv_csr(n, p, i, v, x, y, z, 1.0, 0.0);
+    sym_lib::ltsolve(n, p, i, v, x);
+    sym_lib::spic0_csr(n, v, p, i);
+    sym_lib::parsy::lsolve(n, p, i, v, x);
+    sym_lib::parsy::lus_cr(n, 1, p, i, v, i, x, y);
+    sym_lib::build_levelSet_CSC(1, p, i, lp, ls);
+    delete[] lp; delete[] ls;
+  }
+  std::printf("%s\n", gbsym_status_string(gbsym_last_error()));
+  return 0;
+}
+''')
+    exe = tmp_path / "caller"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run(["g++", "-std=c++11", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                        "-L" + libdir, "-lgbsym", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0 and out.stdout.strip() == "ok", out

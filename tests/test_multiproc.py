@@ -1,0 +1,91 @@
+"""Multi-rank placement of a batch of independent systems, run as two gloo
+ranks on CPU: every system lands on exactly one rank, the loads balance,
+and each rank's shard is solved independently (oracle arithmetic, no data
+exchanged) to the same answer a single rank gives."""
+import os
+import socket
+
+import numpy as np
+import pytest
+import torch.distributed as dist
+import torch.multiprocessing as mp
+
+from sympiler_gb300 import matgen as mg
+from sympiler_gb300.shard import partition_systems, system_cost
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _systems(seed=3, count=12):
+    rng = np.random.default_rng(seed)
+    out = []
+    for q in range(count):
+        A = mg.lap2d(int(rng.integers(5, 40)), int(rng.integers(5, 40)))
+        out.append(mg.tril(A))
+    return out
+
+
+def _worker(rank, world, port, result_dir):
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import oracle
+    import torch
+    orc = oracle.orc()
+    systems = _systems()
+    costs = [system_cost(L.n, L.nnz) for L in systems]
+    mine = partition_systems(costs, world)[rank]
+    # each rank solves only its systems; nothing is exchanged on the data path
+    sums = np.zeros(len(systems))
+    for q in mine:
+        L = systems[q]
+        x = np.ones(L.n)
+        orc.sptrsv_csr(L.n, *L.astuple(), x)
+        sums[q] = x.sum()
+    # gather only for the check
+    t = torch.from_numpy(sums)
+    dist.all_reduce(t)
+    owners = torch.zeros(len(systems), dtype=torch.int64)
+    for q in mine:
+        owners[q] += 1
+    dist.all_reduce(owners)
+    load = torch.tensor([sum(costs[q] for q in mine)], dtype=torch.int64)
+    loads = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+    dist.all_gather(loads, load)
+    if rank == 0:
+        np.save(os.path.join(result_dir, "sums.npy"), t.numpy())
+        np.save(os.path.join(result_dir, "owners.npy"), owners.numpy())
+        np.save(os.path.join(result_dir, "loads.npy"), np.array([int(v.item()) for v in loads]))
+    dist.destroy_process_group()
+
+
+def test_partition_is_exact_cover_and_balanced():
+    costs = [5, 9, 1, 7, 3, 3, 8, 2]
+    parts = partition_systems(costs, 3)
+    flat = sorted(i for p in parts for i in p)
+    assert flat == list(range(len(costs)))
+    loads = [sum(costs[i] for i in p) for p in parts]
+    assert max(loads) <= (4 / 3) * (sum(costs) / 3) + max(costs)
+
+
+def test_two_gloo_ranks_solve_disjoint_shards(tmp_path):
+    world = 2
+    mp.spawn(_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    owners = np.load(tmp_path / "owners.npy")
+    assert np.all(owners == 1)
+    loads = np.load(tmp_path / "loads.npy")
+    assert loads.max() <= 1.34 * loads.mean() + 1
+    import oracle
+    orc = oracle.orc()
+    ref = []
+    for L in _systems():
+        x = np.ones(L.n)
+        orc.sptrsv_csr(L.n, *L.astuple(), x)
+        ref.append(x.sum())
+    assert np.array_equal(np.load(tmp_path / "sums.npy"), np.array(ref))
