@@ -50,6 +50,9 @@ def parse():
     ap.add_argument("--rhs", type=int, default=64)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--extras-only", action="store_true")
+    ap.add_argument("--exec", default="auto",
+                    choices=["auto", "levelset", "syncfree", "oneblock", "persistent", "cluster"],
+                    help="force one executor instead of autotuning (profiling runs)")
     return ap.parse_args()
 
 
@@ -62,7 +65,7 @@ def algorithmic_bytes(nnz_l, n, k, vbytes=8, sbytes=8):
 # FP64 throughput of this machine's GB300 (dependent-free DFMA stream, all SMs):
 # 502 G operations/s, measured by a microbenchmark during development.  On
 # this part the FP64 pipe, not HBM, bounds an FP64 triangular solve.
-FP64_PEAK_GOPS = 502.0
+FP64_PEAK_GOPS = 597.0
 
 
 def fp64_ops_exact(nnz_off, n, k):
@@ -361,7 +364,12 @@ def main():
     L = mg.transpose(Lt)
     plan = TriPlan(L.n, *L.astuple())
     from sympiler_gb300._lib import EXEC_NAMES
-    tuned = {"k1": EXEC_NAMES.get(plan.autotune(k=1)), "k%d" % k: EXEC_NAMES.get(plan.autotune(k=k))}
+    if args.exec == "auto":
+        tuned = {"k1": EXEC_NAMES.get(plan.autotune(k=1)), "k%d" % k: EXEC_NAMES.get(plan.autotune(k=k))}
+    else:
+        forced = {v: c for c, v in EXEC_NAMES.items()}[args.exec]
+        plan.set_exec(forced)
+        tuned = {"k1": args.exec, "k%d" % k: args.exec, "forced": True}
     info = plan.info()
     n = L.n
     byt = algorithmic_bytes(L.nnz, n, k)
@@ -456,8 +464,10 @@ def main():
                          "frac": byt / t_step / 1e9 / peak, "peak_source": peak_src,
                          "traffic": traffic,
                          "algorithmic_bytes_per_solve": byt,
-                         "note": "one launch = one forward solve (graph of per-level kernels); "
-                                 "duration from CUDA events on the launch stream"},
+                         "note": ("one solve = one graph of per-level kernels"
+                                  if tuned["k%d" % k] == "levelset" else
+                                  "one solve = one %s kernel launch" % tuned["k%d" % k])
+                                 + "; duration from CUDA events on the launch stream"},
             "roofline_fp64": {"bound": "fp64 pipe", "achieved": fp64_ops_exact(int(info.nnz_off), n, k) / t_step / 1e9,
                               "peak": FP64_PEAK_GOPS, "unit": "G FP64 op/s",
                               "frac": fp64_ops_exact(int(info.nnz_off), n, k) / t_step / 1e9 / FP64_PEAK_GOPS,

@@ -101,10 +101,12 @@ __device__ __forceinline__ long long clock_now() { return clock64(); }
 constexpr long long kWaitLimitCycles = 1ll << 32;
 
 // G lanes per row; each lane owns the slices r = gl*VEC + s*G*VEC of its
-// row and works on one slice at a time, independently of the other lanes:
-// it polls the values its slice reads and, as soon as all of them are
-// there, computes and publishes its slice.  Warp units hold rows of a
-// single level (units are cut per level).
+// row and works on one slice at a time.  Warp units hold rows of a single
+// level (units are cut per level), so no row of a unit waits on another.
+// Per slice the warp first polls until every lane holds all the values its
+// slice reads -- a loop with no floating-point work, so polling rounds cost
+// the FP64 pipe nothing -- and then each lane computes and publishes its
+// slice once, in storage order.
 template <class T, int G, int VEC, int AR>
 __global__ void __launch_bounds__(kSfBlock)
 k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int *__restrict__ unit_row,
@@ -129,7 +131,6 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
       unsigned got = 0;
       const unsigned need = (1u << ns) - 1u;
       int jo = A.K;          // next overflow dependency
-      bool slab_in = false;  // slab part applied to acc
       T acc[VEC];
       if (!done) vload<T, VEC, false>(x + (size_t)rs.orig * k + r, acc);
       long long t0 = clock_now();
@@ -150,42 +151,14 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
               }
             }
           }
-          if (got == need) {
-            // the slab part in storage order (once), then the overflow
-            // entries as they become ready, still in storage order
-            if (!slab_in) {
-#pragma unroll
-              for (int q = 0; q < kSlabMax; ++q)
-                if (q < ns) {
-#pragma unroll
-                  for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], rs.v[q], xv[q][w]);
-                }
-              slab_in = true;
-            }
-            while (jo < rs.len) {
-              const int e = rs.ovb + jo - A.K;
-              T v[VEC];
-              ld_rlx<T, VEC>(y + (size_t)A.oci[e] * k + r, v);
-              if (!all_ready<T, VEC>(v)) break;
-              const T a = A.ov[e];
-#pragma unroll
-              for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], a, v[w]);
-              ++jo;
-              moved = true;
-            }
-            if (jo >= rs.len) {
-              T out[VEC];
-#pragma unroll
-              for (int w = 0; w < VEC; ++w) {
-                acc[w] = row_finish(A, rs, acc[w]);
-                out[w] = not_sentinel(acc[w]);
-              }
-              vstore<T, VEC>(x + (size_t)rs.orig * k + r, acc);
-              st_rlx<T, VEC>(y + (size_t)rs.orig * k + r, out);
-              done = true;
-              moved = true;
-            }
+          while (jo < rs.len) {
+            T v[VEC];
+            ld_rlx<T, VEC>(y + (size_t)A.oci[rs.ovb + jo - A.K] * k + r, v);
+            if (!all_ready<T, VEC>(v)) break;
+            ++jo;
+            moved = true;
           }
+          if (got == need && jo >= rs.len) done = true;
           if (moved) t0 = clock_now();
         }
         if (!__any_sync(FULL, moved)) __nanosleep(32);  // nothing moved: back off briefly
@@ -197,6 +170,30 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
           const int e = lane == 0 ? ld_relaxed(err) : 0;
           if (__shfl_sync(FULL, e, 0) != 0) return;
         }
+      }
+      if (active && r < k) {
+#pragma unroll
+        for (int q = 0; q < kSlabMax; ++q)
+          if (q < ns) {
+#pragma unroll
+            for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], rs.v[q], xv[q][w]);
+          }
+        for (int t = A.K; t < rs.len; ++t) {
+          const int e = rs.ovb + t - A.K;
+          T v[VEC];
+          ld_rlx<T, VEC>(y + (size_t)A.oci[e] * k + r, v);
+          const T a = A.ov[e];
+#pragma unroll
+          for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], a, v[w]);
+        }
+        T out[VEC];
+#pragma unroll
+        for (int w = 0; w < VEC; ++w) {
+          acc[w] = row_finish(A, rs, acc[w]);
+          out[w] = not_sentinel(acc[w]);
+        }
+        vstore<T, VEC>(x + (size_t)rs.orig * k + r, acc);
+        st_rlx<T, VEC>(y + (size_t)rs.orig * k + r, out);
       }
     }
   }
