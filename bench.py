@@ -421,21 +421,40 @@ def main():
         value_rank = byt / t_step / 1e9
         value = value_rank * world
 
-        # end to end through the C ABI: pinned host buffers, H2D + solve + D2H
+        # end to end through the C ABI on pinned host buffers.  On a coherent
+        # CPU-GPU system the library solves such a buffer in place over the
+        # link (each right-hand side read once, each result written once,
+        # overlapped with the sweep); elsewhere it stages H2D + solve + D2H.
+        # The staged path is timed too (GBSYM_HOST_DIRECT=0) for comparison.
+        from sympiler_gb300.plans import host_solve_in_place
         Hb = torch.empty((n, k), dtype=torch.float64).pin_memory()
         Hb.copy_(B.cpu())
         Hx = torch.empty_like(Hb).pin_memory()
-        for _ in range(2):
-            Hx.copy_(Hb)
-            plan.solve_host_ptr(Hx.data_ptr(), k)
-        e2e_t = []
-        for _ in range(max(3, args.steps // 2)):
-            Hx.copy_(Hb)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            plan.solve_host_ptr(Hx.data_ptr(), k)
-            e2e_t.append(time.perf_counter() - t0)
-        e2e_step = statistics.median(e2e_t)
+
+        def e2e_median(direct):
+            if direct:
+                os.environ.pop("GBSYM_HOST_DIRECT", None)
+            else:
+                os.environ["GBSYM_HOST_DIRECT"] = "0"
+            for _ in range(2):
+                Hx.copy_(Hb)
+                plan.solve_host_ptr(Hx.data_ptr(), k)
+            ts = []
+            for _ in range(max(3, args.steps // 2)):
+                Hx.copy_(Hb)
+                flush.fill_(rank + 1)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                plan.solve_host_ptr(Hx.data_ptr(), k)
+                ts.append(time.perf_counter() - t0)
+            os.environ.pop("GBSYM_HOST_DIRECT", None)
+            return statistics.median(ts)
+
+        e2e_staged = e2e_median(False)
+        e2e_step = e2e_median(True)
+        in_place = host_solve_in_place(Hx.data_ptr())
+        # the in-place result must equal the device-resident one bit for bit
+        e2e_exact = bool(torch.equal(Hx, X.cpu()))
 
         # parity spot check of the timed result (first column) against a
         # plain FP64 dense-free check: residual of L x = b on one column
@@ -475,7 +494,12 @@ def main():
                               "peak_source": "measured (DFMA throughput microbenchmark, this pool)"},
             "e2e": {"value": byt / e2e_step / 1e9, "unit": UNIT, "h2d_bytes_per_step": n * k * 8,
                     "d2h_bytes_per_step": n * k * 8, "ms_per_step": e2e_step * 1e3,
-                    "api": "gbsym_tri_solve_host (pinned host x, row-major)"},
+                    "api": "gbsym_tri_solve_host (pinned host x, row-major, wall clock per call)",
+                    "path": ("in place over the CPU-GPU link (sync-free sweep reads b and writes x "
+                             "in the host buffer)") if in_place else "staged: H2D + solve + D2H",
+                    "bit_identical_to_device_solve": e2e_exact,
+                    "staged_ms_per_step": e2e_staged * 1e3,
+                    "staged_value": byt / e2e_staged / 1e9},
             "gpu_launches": int(launches),
             "clocks": clocks,
             "check": {"max_abs_residual_col0": resid},

@@ -246,9 +246,18 @@ int gbsym_tri_solve(gbsym_tri t, void *x, int k, int layout, int dtype,
                     void *stream);
 /* The lbc_redundant row formula: x_i = ((0 - sum_j L_ij x_j) + b_i)/L_ii. */
 int gbsym_tri_solve_b(gbsym_tri t, const double *b, double *x, void *stream);
-/* End-to-end: x is HOST memory (pinned or pageable), copied in, solved and
- * copied back before the call returns. */
+/* End-to-end: x is HOST memory (pinned or pageable); the call returns when
+ * the solution is in x.  Pageable memory, and any memory on a system whose
+ * GPU does not share the CPU's page tables, is staged: copied in, solved,
+ * copied back.  Page-locked memory on a coherent CPU-GPU system (Grace with
+ * NVLink-C2C) is solved in place: the sync-free sweep reads each right-hand
+ * side and writes each result directly in the caller's buffer, so the
+ * transfers overlap the sweep instead of preceding and following it
+ * (row-major layout, or k = 1).  Results are identical either way. */
 int gbsym_tri_solve_host(gbsym_tri t, double *x, int k, int layout);
+/* 1 if gbsym_tri_solve_host would solve the host buffer x in place (it is
+ * page-locked and the current GPU shares the CPU's page tables), else 0. */
+int gbsym_host_solve_in_place(const void *x);
 
 /* ---- CSR matrix plan (SpMV) -------------------------------------------- */
 typedef struct gbsym_csr_s *gbsym_csr;

@@ -71,6 +71,7 @@ SIGNATURES = {
     "gbsym_tri_solve": (_int, [_vp, _vp, _int, _int, _int, _vp]),
     "gbsym_tri_solve_b": (_int, [_vp, _vp, _vp, _vp]),
     "gbsym_tri_solve_host": (_int, [_vp, _vp, _int, _int]),
+    "gbsym_host_solve_in_place": (_int, [_vp]),
     "gbsym_csr_create": (_int, [C.POINTER(_vp), _int, _int, _vp, _vp, _vp, _int, _int, _vp]),
     "gbsym_csr_destroy": (_int, [_vp]),
     "gbsym_csr_spmv": (_int, [_vp, _vp, _vp, _int, _vp]),

@@ -566,6 +566,9 @@ void gather_values(long long m, const double *src, const int *idx, double *dst, 
   check_launch();
 }
 
+template <class T>
+void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s);  // exec_syncfree.cu
+
 }  // namespace gbsym
 
 // ---------------------------------------------------------------------------
@@ -719,10 +722,52 @@ extern "C" int gbsym_tri_solve_b(gbsym_tri t, const double *b, double *x, void *
   });
 }
 
+// Device pointer through which kernels may read and write the page-locked
+// host buffer p in place, or null when the buffer must be staged: p is not
+// page-locked, or the GPU does not share the CPU's page tables (a PCIe
+// system, where zero-copy access would run at link latency per access).
+// GBSYM_HOST_DIRECT=0 forces staging.
+static void *host_direct_pointer(void *p) {
+  const char *e = std::getenv("GBSYM_HOST_DIRECT");
+  if (e && e[0] == '0') return nullptr;
+  int dev = 0, coherent = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  GB_CUDA(cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev));
+  if (!coherent) return nullptr;
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  return a.devicePointer;
+}
+
+extern "C" int gbsym_host_solve_in_place(const void *x) {
+  int r = 0;
+  if (!x) return 0;
+  const int st = guarded([&] { r = host_direct_pointer(const_cast<void *>(x)) != nullptr; });
+  return st ? 0 : r;
+}
+
 extern "C" int gbsym_tri_solve_host(gbsym_tri t, double *x, int k, int layout) {
   if (!t || (!x && t->n && k)) return GBSYM_ERR_NULL_ARG;
+  if (k < 0) return GBSYM_ERR_SIZE;
   return guarded([&] {
     cudaStream_t s = thread_stream();
+    if (t->n == 0 || k == 0) return;
+    GB_CHECK(t->vdtype == GBSYM_F64, GBSYM_ERR_UNSUPPORTED);
+    if (k == 1 || layout == GBSYM_ROW_MAJOR) {
+      if (void *dp = host_direct_pointer(x)) {
+        // in place over the CPU-GPU link: the sync-free sweep reads each
+        // right-hand side once and writes each result once, and rows
+        // exchange values through its device scratch, never through x
+        run_syncfree<double>(t, static_cast<double *>(dp), k, s);
+        const int code = tri_read_error(t, s);
+        if (code) throw Err{code};
+        return;
+      }
+    }
     const size_t bytes = (size_t)t->n * k * sizeof(double);
     t->io.reserve(bytes);
     double *dx = (double *)t->io.p;

@@ -181,6 +181,12 @@ class TriPlan:
             pass
 
 
+def host_solve_in_place(ptr: int) -> bool:
+    """True if a host-buffer solve on ``ptr`` runs in place over the CPU-GPU
+    link (page-locked memory on a coherent system) rather than staged."""
+    return bool(lib().gbsym_host_solve_in_place(C.c_void_p(ptr)))
+
+
 class CsrPlan:
     """A CSR matrix resident on the GPU for SpMV."""
 

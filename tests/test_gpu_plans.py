@@ -166,6 +166,30 @@ def test_column_major_and_host_solve(gpu, orc, c2_factor):
     assert np.array_equal(h, ref)
 
 
+@pytest.mark.parametrize("k", [1, 8, 64])
+@pytest.mark.parametrize("pinned", [True, False])
+def test_host_solve_in_place_and_staged(gpu, orc, c2_factor, k, pinned):
+    """Row-major host buffers: page-locked memory is solved in place over the
+    CPU-GPU link where the system is coherent, pageable memory is staged;
+    both must give the oracle's bits, twice in a row on one plan."""
+    from sympiler_gb300._lib import ROW_MAJOR
+    from sympiler_gb300.plans import TriPlan
+    _, L, _ = c2_factor
+    rng = np.random.default_rng(100 + k)
+    B = rng.standard_normal((L.n, k))
+    ref = _oracle_mrhs(orc, L, B)
+    plan = TriPlan(L.n, *L.astuple())
+    for _ in range(2):
+        if pinned:
+            h = torch.from_numpy(B.copy()).pin_memory()
+            plan.solve_host_ptr(h.data_ptr(), k, layout=ROW_MAJOR)
+            got = h.numpy()
+        else:
+            got = B.copy()
+            plan.solve_host(got, layout=ROW_MAJOR)
+        assert np.array_equal(got.reshape(L.n, k), ref)
+
+
 def test_plan_from_device_arrays_and_schedule(gpu, orc):
     from sympiler_gb300.plans import TriPlan
     A = mg.lap2d(100)
