@@ -156,6 +156,42 @@ int gbsym_build_levelset_csr(int n, const int *Lp, const int *Li,
 int gbsym_build_levelset_upper_csr(int n, const int *Up, const int *Ui,
                                    int **level_ptr, int **level_set);
 
+/* LBC schedule inspectors (host code; no GPU needed).  Their outputs feed
+ * gbsym_sptrsv_csr_lbc / _ilu_lbc / _lbc_redundant / _csc_lbc and
+ * gbsym_parsy_lsolveParH2: level_ptr[level_no+1] indexes part_ptr,
+ * part_ptr[part_no+1] indexes node_ptr[n].
+ *
+ * Replaces parsy::getLevelSet (sparse_blas/parsy/common/TreeUtils.cpp:89-140):
+ * level set of a forest (parent[v] > v, or -1 for a root), leaves first,
+ * ascending index within a level.  level_ptr (n+1 ints) and level_set (n
+ * ints) are caller-allocated, as in the reference.  Returns level_no, or
+ * -status. */
+int gbsym_tree_levelset(int n, const int *parent, int *level_ptr, int *level_set);
+/* Replaces parsy::getCoarseLevelSet_6
+ * (sparse_blas/parsy/symbolic/InspectionLevel_06.cpp:17-400): tree LBC of a
+ * forest with per-node costs; inner_parts, min_level_dist and div_rate mean
+ * what innerParts, minLevelDist and divRate mean there.  *level_ptr,
+ * *part_ptr (n+1 ints each) and *node_ptr (n ints) are allocated here;
+ * release them with gbsym_free. */
+int gbsym_coarse_levelset_tree(int n, const int *parent, const double *node_cost,
+                               int inner_parts, int min_level_dist, int div_rate,
+                               int *level_no, int **level_ptr, int *part_no,
+                               int **part_ptr, int **node_ptr);
+/* Replaces get_coarse_levelSet_DAG_CSC_tree at its call site
+ * (demo/sptrsv_demo_utils.h:78-90; the function lives in the unvendored
+ * aggregation dependency): LBC of the solve DAG of L, given as the CSR of a
+ * lower triangle.  The tree LBC runs on the elimination tree of L's
+ * symmetric pattern, which orders every dependency of the solve.  cost may
+ * be NULL for the demo's cost, the entries per row.  Outputs as
+ * gbsym_coarse_levelset_tree. */
+int gbsym_build_lbc(int n, const int *Lp, const int *Li, const double *cost,
+                    int inner_parts, int min_level_dist, int div_rate,
+                    int *level_no, int **level_ptr, int *part_no,
+                    int **part_ptr, int **node_ptr);
+/* Elimination tree of the symmetric matrix whose lower triangle has the
+ * pattern of the CSR (Lp, Li): parent[n], -1 at roots. */
+int gbsym_etree_lower_csr(int n, const int *Lp, const int *Li, int *parent);
+
 /* ======================================================================== */
 /* Plans (device-resident).                                                 */
 /* ======================================================================== */

@@ -106,7 +106,61 @@ inline int build_levelSet_CSC(size_t n, const int *Lp, const int *Li, int *&leve
   return nl;
 }
 
+namespace detail {
+// Copy an LBC result from gbsym_free'd buffers into new[] arrays sized as
+// the reference sizes them (level and part pointers n+1, nodes n).
+inline void lbc_to_new(size_t n, int st, int nl, int *lp, int np, int *pp, int *nd, int &level_no,
+                       int *&level_ptr, int &part_no, int *&part_ptr, int *&node_ptr) {
+  level_ptr = new int[n + 1]();
+  part_ptr = new int[n + 1]();
+  node_ptr = new int[n > 0 ? n : 1]();
+  level_no = 0;
+  part_no = 0;
+  if (st == GBSYM_OK && n > 0) {
+    level_no = nl;
+    part_no = np;
+    std::memcpy(level_ptr, lp, sizeof(int) * (size_t)(nl + 1));
+    std::memcpy(part_ptr, pp, sizeof(int) * (size_t)(np + 1));
+    std::memcpy(node_ptr, nd, sizeof(int) * n);
+  }
+  gbsym_free(lp);
+  gbsym_free(pp);
+  gbsym_free(nd);
+}
+}  // namespace detail
+
+// LBC of the solve DAG of a lower CSR, at the reference demo's call site
+// (demo/sptrsv_demo_utils.h:78-90; the function belongs to the unvendored
+// aggregation dependency).  lp = parts per coarse level, cp = minimum level
+// distance, ic = division rate; stype is unused.  Outputs are new[] arrays.
+inline int get_coarse_levelSet_DAG_CSC_tree(size_t n, const int *Lp, const int *Li, int /*stype*/,
+                                            int &final_level_no, int *&fina_level_ptr, int &part_no,
+                                            int *&final_part_ptr, int *&final_node_ptr, int lp, int cp,
+                                            int ic, double *cost) {
+  int nl = 0, np = 0, *a = nullptr, *b = nullptr, *c = nullptr;
+  const int st = gbsym_build_lbc((int)n, Lp, Li, cost, lp, cp, ic, &nl, &a, &np, &b, &c);
+  detail::lbc_to_new(n, st, nl, a, np, b, c, final_level_no, fina_level_ptr, part_no, final_part_ptr,
+                     final_node_ptr);
+  return st == GBSYM_OK ? final_level_no : -st;
+}
+
 namespace parsy {
+// TreeUtils.h getLevelSet (TreeUtils.cpp:89-140): caller-allocated arrays.
+inline int getLevelSet(size_t n, const int *inTree, int *levelPtr, int *levelSet) {
+  return gbsym_tree_levelset((int)n, inTree, levelPtr, levelSet);
+}
+// InspectionLevel_06.h:13 (InspectionLevel_06.cpp:17-400); blk2col and
+// parLevelSet are unused, as in the reference.
+inline int getCoarseLevelSet_6(size_t n, const int *eTree, const int * /*blk2col*/, int &finaLevelNo,
+                               int *&finaLevelPtr, int *& /*parLevelSet*/, int &partNo, int *&finalPartPtr,
+                               int *&finalNodePtr, int innerParts, int minLevelDist, int divRate,
+                               double *nodeCost) {
+  int nl = 0, np = 0, *a = nullptr, *b = nullptr, *c = nullptr;
+  const int st = gbsym_coarse_levelset_tree((int)n, eTree, nodeCost, innerParts, minLevelDist, divRate, &nl,
+                                            &a, &np, &b, &c);
+  detail::lbc_to_new(n, st, nl, a, np, b, c, finaLevelNo, finaLevelPtr, partNo, finalPartPtr, finalNodePtr);
+  return finaLevelNo;
+}
 // Triangular_CSC.h:14-36
 inline int lsolve(int n, int *Lp, int *Li, double *Lx, double *x) {
   return gbsym_parsy_lsolve(n, Lp, Li, Lx, x);

@@ -72,6 +72,10 @@ SIGNATURES = {
     "gbsym_tri_solve_b": (_int, [_vp, _vp, _vp, _vp]),
     "gbsym_tri_solve_host": (_int, [_vp, _vp, _int, _int]),
     "gbsym_host_solve_in_place": (_int, [_vp]),
+    "gbsym_tree_levelset": (_int, [_int, _vp, _vp, _vp]),
+    "gbsym_coarse_levelset_tree": (_int, [_int, _vp, _vp, _int, _int, _int, _vp, _vp, _vp, _vp, _vp]),
+    "gbsym_build_lbc": (_int, [_int, _vp, _vp, _vp, _int, _int, _int, _vp, _vp, _vp, _vp, _vp]),
+    "gbsym_etree_lower_csr": (_int, [_int, _vp, _vp, _vp]),
     "gbsym_csr_create": (_int, [C.POINTER(_vp), _int, _int, _vp, _vp, _vp, _int, _int, _vp]),
     "gbsym_csr_destroy": (_int, [_vp]),
     "gbsym_csr_spmv": (_int, [_vp, _vp, _vp, _int, _vp]),

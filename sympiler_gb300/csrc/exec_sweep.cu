@@ -201,7 +201,6 @@ static void persist_ar(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
 template <class T>
 void run_persist(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
   GB_CUDA(cudaMemsetAsync(t->bar.p, 0, sizeof(unsigned), s));
-  count_launch();
   if (t->arith == kArithFused) persist_ar<T, kArithFused>(t, x, k, s);
   else persist_ar<T, kArithExact>(t, x, k, s);
 }

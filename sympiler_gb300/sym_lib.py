@@ -170,6 +170,28 @@ class parsy:  # noqa: N801 -- mirrors the reference's nested namespace
                                              parts, _p(pp), _p(pa), chunk)
 
     @staticmethod
+    def getLevelSet(n, inTree, levelPtr, levelSet):  # noqa: N802,N803
+        """sparse_blas/parsy/common/TreeUtils.cpp:89-140 -- level set of a
+        forest into caller arrays levelPtr (n+1) and levelSet (n); returns
+        the level count."""
+        t = _arr(inTree, _I32, "inTree")
+        lp, ls = _arr(levelPtr, _I32, "levelPtr", True), _arr(levelSet, _I32, "levelSet", True)
+        nl = lib().gbsym_tree_levelset(int(n), _p(t), _p(lp), _p(ls))
+        if nl < 0:
+            raise GbsymError(-nl, "getLevelSet")
+        return nl
+
+    @staticmethod
+    def getCoarseLevelSet_6(n, eTree, blk2col, innerParts, minLevelDist, divRate,  # noqa: N802,N803
+                            nodeCost):
+        """sparse_blas/parsy/symbolic/InspectionLevel_06.cpp:17-400 -- tree
+        LBC.  blk2col is accepted and unused, as in the reference.  Returns
+        (finaLevelNo, finaLevelPtr, partNo, finalPartPtr, finalNodePtr)."""
+        return _lbc_call(lib().gbsym_coarse_levelset_tree, n,
+                         (_arr(eTree, _I32, "eTree"), _arr(nodeCost, _F64, "nodeCost")),
+                         innerParts, minLevelDist, divRate, "getCoarseLevelSet_6")
+
+    @staticmethod
     def lus_cr(n, nz_num, ia, ja, l, ua, r, z):
         """sparse_blas/parsy/gmres/mgmres.cpp:598-689 -- z = (LU)^{-1} r."""
         ia, ja, ua = _arr(ia, _I32, "ia"), _arr(ja, _I32, "ja"), _arr(ua, _I32, "ua")
@@ -254,3 +276,47 @@ def build_levelset_csr(n, Lp, Li):
 
 def build_levelset_upper_csr(n, Up, Ui):
     return _levels(lib().gbsym_build_levelset_upper_csr, n, Up, Ui, "build_levelset_upper_csr")
+
+
+# ---- LBC inspectors ---------------------------------------------------------
+
+def _lbc_call(fn, n, arrays, inner_parts, min_level_dist, div_rate, where):
+    nl, pn = C.c_int(0), C.c_int(0)
+    lp, pp, nd = C.POINTER(C.c_int)(), C.POINTER(C.c_int)(), C.POINTER(C.c_int)()
+    st = fn(int(n), *[_p(a) for a in arrays], int(inner_parts), int(min_level_dist), int(div_rate),
+            C.byref(nl), C.byref(lp), C.byref(pn), C.byref(pp), C.byref(nd))
+    if st != 0:
+        raise GbsymError(st, where)
+    if n == 0:
+        z = np.zeros(1, dtype=_I32)
+        return 0, z, 0, z.copy(), np.zeros(0, dtype=_I32)
+    try:
+        level_ptr = np.ctypeslib.as_array(lp, shape=(nl.value + 1,)).copy()
+        part_ptr = np.ctypeslib.as_array(pp, shape=(pn.value + 1,)).copy()
+        node_ptr = np.ctypeslib.as_array(nd, shape=(n,)).copy()
+    finally:
+        for q in (lp, pp, nd):
+            lib().gbsym_free(C.cast(q, C.c_void_p))
+    return nl.value, level_ptr, pn.value, part_ptr, node_ptr
+
+
+def get_coarse_levelSet_DAG_CSC_tree(n, Lp, Li, stype, lp, cp, ic, cost=None):  # noqa: N802
+    """LBC of the solve DAG of the lower CSR (Lp, Li), as the reference demo
+    calls it (demo/sptrsv_demo_utils.h:78-90): lp = parts per coarse level,
+    cp = minimum level distance, ic = division rate; cost defaults to the
+    entries per row.  stype is accepted and unused.  Returns (level_no,
+    level_ptr, part_no, part_ptr, node_ptr)."""
+    arrays = (_arr(Lp, _I32, "Lp"), _arr(Li, _I32, "Li"),
+              None if cost is None else _arr(cost, _F64, "cost"))
+    return _lbc_call(lib().gbsym_build_lbc, n, arrays, lp, cp, ic, "get_coarse_levelSet_DAG_CSC_tree")
+
+
+def etree_lower_csr(n, Lp, Li):
+    """Elimination tree (parent array, -1 at roots) of the symmetric matrix
+    whose lower triangle has the pattern of the CSR (Lp, Li)."""
+    Lp, Li = _arr(Lp, _I32, "Lp"), _arr(Li, _I32, "Li")
+    parent = np.zeros(max(int(n), 1), dtype=_I32)
+    st = lib().gbsym_etree_lower_csr(int(n), _p(Lp), _p(Li), _p(parent))
+    if st != 0:
+        raise GbsymError(st, "etree_lower_csr")
+    return parent[: int(n)]

@@ -1,9 +1,12 @@
 """The C-ABI library loads and exports every entry point include/gbsym.h
-declares (no compute call: this runs without a GPU)."""
+declares; the host-only entry points (schedule inspectors, status strings)
+run here without a GPU."""
 import ctypes
 import os
 import re
 import subprocess
+
+import numpy as np
 
 from conftest import ROOT
 
@@ -82,3 +85,53 @@ int main(int argc, char **argv) {
     assert r.returncode == 0, r.stderr
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0 and out.stdout.strip() == "ok", out
+
+
+def test_cpp_shim_runs_lbc_inspectors(tmp_path):
+    """The inspectors are host code: a C++ caller of the reference's
+    signatures runs them here and gets what the Python binding gets."""
+    from sympiler_gb300 import _lib, sym_lib
+    from sympiler_gb300 import matgen as mg
+    L = mg.tril(mg.random_spd(300, 3, np.random.default_rng(4)))
+    src = tmp_path / "inspect.cpp"
+    arr = lambda a: ",".join(str(int(v)) for v in a)  # noqa: E731
+    src.write_text(r'''
+#include "gbsym_sym_lib.hpp"
+#include <cstdio>
+static const int Lp[] = {%s};
+static const int Li[] = {%s};
+int main() {
+  const int n = %d;
+  int nl = 0, np = 0, *lp = nullptr, *pp = nullptr, *nd = nullptr;
+  double *cost = nullptr;
+  sym_lib::get_coarse_levelSet_DAG_CSC_tree(n, Lp, Li, 0, nl, lp, np, pp, nd, 4, -1, 100, cost);
+  std::printf("%%d %%d\n", nl, np);
+  for (int i = 0; i <= nl; ++i) std::printf("%%d ", lp[i]);
+  std::printf("\n");
+  for (int i = 0; i <= np; ++i) std::printf("%%d ", pp[i]);
+  std::printf("\n");
+  for (int i = 0; i < n; ++i) std::printf("%%d ", nd[i]);
+  std::printf("\n");
+  delete[] lp; delete[] pp; delete[] nd;
+  int parent[n], tlp[n + 1], tls[n];
+  gbsym_etree_lower_csr(n, Lp, Li, parent);
+  std::printf("%%d\n", sym_lib::parsy::getLevelSet(n, parent, tlp, tls));
+  return 0;
+}
+''' % (arr(L.p), arr(L.i), L.n))
+    exe = tmp_path / "inspect"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run(["g++", "-std=c++11", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe),
+                        "-L" + libdir, "-lgbsym", "-Wl,-rpath," + libdir], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    lines = out.stdout.split("\n")
+    nl, lp, pn, pp, nodes = sym_lib.get_coarse_levelSet_DAG_CSC_tree(L.n, L.p, L.i, 0, 4, -1, 100)
+    assert lines[0].split() == [str(nl), str(pn)]
+    assert [int(v) for v in lines[1].split()] == list(lp)
+    assert [int(v) for v in lines[2].split()] == list(pp)
+    assert [int(v) for v in lines[3].split()] == list(nodes)
+    par = sym_lib.etree_lower_csr(L.n, L.p, L.i)
+    tlp, tls = np.zeros(L.n + 1, np.int32), np.zeros(L.n, np.int32)
+    assert int(lines[4]) == sym_lib.parsy.getLevelSet(L.n, par, tlp, tls)

@@ -130,6 +130,24 @@ def test_lbc_schedule_from_reference(gpu, orc):
     assert np.array_equal(x, d["x_serial"])
 
 
+def test_dag_lbc_schedule_drives_gpu_drop_ins(gpu, orc):
+    """The library's own DAG LBC inspector feeding its LBC drop-ins, as the
+    reference demo chains get_coarse_levelSet_DAG_CSC_tree into
+    sptrsv_csr_lbc: results equal the serial oracle's bits."""
+    from sympiler_gb300 import sym_lib
+    d = golden("ic0_random_spd_2000")
+    n = len(d["Up"]) - 1
+    L = mg.transpose(mg.CSR(n, d["Up"], d["Ui"], d["factor"]))
+    for parts in (2, 6, 64):
+        nl, lp, pn, pp, nodes = sym_lib.get_coarse_levelSet_DAG_CSC_tree(n, L.p, L.i, 0, parts, -1, 100)
+        x = d["b"].copy()
+        sym_lib.sptrsv_csr_lbc(n, *L.astuple(), x, nl, lp, pp, nodes)
+        assert np.array_equal(x, d["x_serial"])
+        x = d["b"].copy()
+        sym_lib.sptrsv_csc_lbc(n, d["Up"], d["Ui"], d["factor"], x, nl, lp, pp, nodes)
+        assert np.array_equal(x, d["x_serial"])
+
+
 def test_ilu_solves(gpu, orc):
     from sympiler_gb300 import sym_lib
     d = golden("ilu0_convdiff_8")
