@@ -214,7 +214,7 @@ def cpu_baseline_sample(L, k, nl, lp, ls):
     X = B.copy()
     orc.sptrsv_csr_levelset_mrhs(L.n, *L.astuple(), X, cols, nl, lp, ls, cores)  # warm
     reps, t_tot = 0, 0.0
-    while t_tot < 3.0 and reps < 50:
+    while t_tot < 10.0 and reps < 400:
         X = B.copy()
         t0 = time.perf_counter()
         orc.sptrsv_csr_levelset_mrhs(L.n, *L.astuple(), X, cols, nl, lp, ls, cores)

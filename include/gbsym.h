@@ -215,9 +215,13 @@ enum gbsym_exec {
   GBSYM_EXEC_SYNCFREE = 2,  /* one persistent launch, per-row ready flags  */
   GBSYM_EXEC_ONEBLOCK = 3,  /* one thread block sweeps all levels          */
   GBSYM_EXEC_PERSISTENT = 4, /* one cooperative launch, grid barrier/level */
-  GBSYM_EXEC_CLUSTER = 5     /* thread-block clusters, hardware cluster
+  GBSYM_EXEC_CLUSTER = 5,    /* thread-block clusters, hardware cluster
                                 barrier per level; k > 1 splits columns
                                 over clusters                             */
+  GBSYM_EXEC_PARTITIONED = 6 /* contiguous row partitions, one block each:
+                                dependencies inside a partition through
+                                shared memory, across partitions sync-free
+                                (k = 1; k > 1 runs SYNCFREE)              */
 };
 
 /* Arithmetic of the row updates.  EXACT: every x_i -= L_ij x_j is a

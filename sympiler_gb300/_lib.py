@@ -125,9 +125,9 @@ OK, ERR_NULL_ARG, ERR_BAD_SCHEDULE, ERR_PIVOT, ERR_TIMEOUT, ERR_CUDA, ERR_BAD_MA
 LOWER_DIAG_LAST, UPPER_DIAG_FIRST, ILU_UNIT_LOWER, ILU_UPPER, ILU_LOWER_DIV, LOWER_CSC = range(6)
 F64, F32 = 0, 1
 COL_MAJOR, ROW_MAJOR = 0, 1
-EXEC_AUTO, EXEC_LEVELSET, EXEC_SYNCFREE, EXEC_ONEBLOCK, EXEC_PERSISTENT, EXEC_CLUSTER = range(6)
+EXEC_AUTO, EXEC_LEVELSET, EXEC_SYNCFREE, EXEC_ONEBLOCK, EXEC_PERSISTENT, EXEC_CLUSTER, EXEC_PARTITIONED = range(7)
 EXEC_NAMES = {EXEC_LEVELSET: "levelset", EXEC_SYNCFREE: "syncfree", EXEC_ONEBLOCK: "oneblock",
-              EXEC_PERSISTENT: "persistent", EXEC_CLUSTER: "cluster"}
+              EXEC_PERSISTENT: "persistent", EXEC_CLUSTER: "cluster", EXEC_PARTITIONED: "partitioned"}
 ARITH_EXACT, ARITH_FUSED = 0, 1
 
 

@@ -33,7 +33,7 @@ static TuneKey tune_key(const gbsym_tri_s *t, int k, int dtype) {
 int effective_exec(const gbsym_tri_s *t, int k, bool redundant) {
   int e = t->exec_forced != GBSYM_EXEC_AUTO ? t->exec_forced : (k == 1 ? t->exec : t->exec_mrhs);
   if (redundant) e = GBSYM_EXEC_LEVELSET;
-  if (e == GBSYM_EXEC_ONEBLOCK && k != 1) e = GBSYM_EXEC_SYNCFREE;
+  if ((e == GBSYM_EXEC_ONEBLOCK || e == GBSYM_EXEC_PARTITIONED) && k != 1) e = GBSYM_EXEC_SYNCFREE;
   if (t->nlev <= 1) e = GBSYM_EXEC_LEVELSET;
   return e;
 }
@@ -56,11 +56,13 @@ void choose_exec(gbsym_tri_s *t) {
     else if (!std::strcmp(force, "oneblock")) e = GBSYM_EXEC_ONEBLOCK;
     else if (!std::strcmp(force, "syncfree")) e = GBSYM_EXEC_SYNCFREE;
     else if (!std::strcmp(force, "cluster")) e = GBSYM_EXEC_CLUSTER;
+    else if (!std::strcmp(force, "partitioned")) e = GBSYM_EXEC_PARTITIONED;
     if (e >= 0) {
       t->exec = e;
-      t->exec_mrhs = e == GBSYM_EXEC_ONEBLOCK ? GBSYM_EXEC_SYNCFREE : e;
+      t->exec_mrhs = (e == GBSYM_EXEC_ONEBLOCK || e == GBSYM_EXEC_PARTITIONED) ? GBSYM_EXEC_SYNCFREE : e;
     }
   }
+  if (const char *pr = std::getenv("GBSYM_PART_ROWS")) t->part_rows_pref = std::atoi(pr);
   if (const char *pb = std::getenv("GBSYM_PERSIST_BLOCKS")) t->persist_blocks = std::atoi(pb);
   if (const char *cb = std::getenv("GBSYM_CLUSTER_BLOCKS")) t->cluster_blocks = std::atoi(cb);
   if (const char *sb = std::getenv("GBSYM_SF_BLOCKS_PER_SM")) t->sf_blocks_per_sm = std::atoi(sb);
@@ -73,6 +75,7 @@ static void solve_as(gbsym_tri_s *t, int e, T *x, const T *b, int k, int dtype, 
     case GBSYM_EXEC_PERSISTENT: run_persist<T>(t, x, k, s); break;
     case GBSYM_EXEC_SYNCFREE: run_syncfree<T>(t, x, k, s); break;
     case GBSYM_EXEC_CLUSTER: run_cluster<T>(t, x, k, s); break;
+    case GBSYM_EXEC_PARTITIONED: run_part<T>(t, x, s); break;
     default: run_levelset<T>(t, x, b, k, dtype, s); break;
   }
 }
@@ -112,19 +115,39 @@ template <class T>
 static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   const long long m = (long long)t->n * k;
   DBuf<T> buf(m);
-  std::vector<int> cands = {GBSYM_EXEC_LEVELSET, GBSYM_EXEC_PERSISTENT, GBSYM_EXEC_SYNCFREE,
-                            GBSYM_EXEC_CLUSTER};
-  if (k == 1 && t->max_level_rows <= 4096) cands.push_back(GBSYM_EXEC_ONEBLOCK);
+  // (executor, partition rows) candidates; the partitioned executor is
+  // tried at several partition sizes (k = 1 only)
+  std::vector<std::pair<int, int>> cands = {{GBSYM_EXEC_LEVELSET, 0}, {GBSYM_EXEC_PERSISTENT, 0},
+                                            {GBSYM_EXEC_SYNCFREE, 0}, {GBSYM_EXEC_CLUSTER, 0}};
+  if (k == 1 && t->max_level_rows <= 4096) cands.push_back({GBSYM_EXEC_ONEBLOCK, 0});
+  if (k == 1) {
+    std::vector<int> sizes;
+    for (int parts : {num_sms() / 4, num_sms() / 2, num_sms(), 2 * num_sms(), 4 * num_sms()}) {
+      const int r = std::min(std::max(64, div_up(t->n, std::max(1, parts))), (200 * 1024) / (int)sizeof(T));
+      if (std::find(sizes.begin(), sizes.end(), r) == sizes.end()) sizes.push_back(r);
+    }
+    for (int r : sizes) cands.push_back({GBSYM_EXEC_PARTITIONED, r});
+  }
+  // caches are flushed between timed runs, as between solves of a longer
+  // computation
+  int l2 = 0, dev = 0;
+  GB_CUDA(cudaGetDevice(&dev));
+  GB_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev));
+  DBuf<char> flush((size_t)std::max(l2, 1 << 20) * 2);
   cudaEvent_t e0, e1;
   GB_CUDA(cudaEventCreate(&e0));
   GB_CUDA(cudaEventCreate(&e1));
-  int best = -1;
+  int best = -1, best_rows = 0;
   float best_ms = 0;
-  for (int e : cands) {
+  const int saved_rows = t->part_rows_pref;
+  for (const auto &cand : cands) {
+    const int e = cand.first;
+    if (e == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = cand.second;
     std::vector<float> ms;
     for (int rep = 0; rep < 4; ++rep) {
       k_fill_tune<T><<<(int)std::min<long long>(div_up(m, 256), num_sms() * 8), 256, 0, s>>>(buf.p, m);
       check_launch();
+      GB_CUDA(cudaMemsetAsync(flush.p, rep, flush.n, s));
       GB_CUDA(cudaEventRecord(e0, s));
       solve_as<T>(t, e, buf.p, nullptr, k, dtype, s);
       GB_CUDA(cudaEventRecord(e1, s));
@@ -138,12 +161,15 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
     const float med = ms[ms.size() / 2];
     if (best < 0 || med < best_ms) {
       best = e;
+      best_rows = cand.second;
       best_ms = med;
     }
   }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  t->part_rows_pref = saved_rows;
   if (best < 0) throw Err{GBSYM_ERR_TIMEOUT};
+  if (best == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = best_rows;
   if (k == 1) t->exec = best; else t->exec_mrhs = best;
   std::lock_guard<std::mutex> lk(g_tuned_mu);
   g_tuned[tune_key(t, k, dtype)] = best;

@@ -236,6 +236,8 @@ void run_oneblock(gbsym_tri_s *t, T *x, cudaStream_t s);
 template <class T>
 void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s);
 template <class T>
+void run_part(gbsym_tri_s *t, T *x, cudaStream_t s);
+template <class T>
 void run_cluster(gbsym_tri_s *t, T *x, int k, cudaStream_t s);
 
 }  // namespace gbsym

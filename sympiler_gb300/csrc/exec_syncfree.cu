@@ -279,17 +279,21 @@ __global__ void k_fill_sentinel(uint4 *__restrict__ p, size_t n16, unsigned *__r
   if (blockIdx.x == 0 && (int)threadIdx.x < ntail) tail[threadIdx.x] = ~0u;
 }
 
+void fill_sentinel(void *y, size_t bytes, cudaStream_t s) {
+  const size_t n16 = bytes / 16;
+  const int ntail = (int)((bytes - n16 * 16) / 4);
+  const int grid = (int)std::max<size_t>(1, std::min<size_t>(div_up(n16, (size_t)256), (size_t)num_sms() * 8));
+  k_fill_sentinel<<<grid, 256, 0, s>>>(reinterpret_cast<uint4 *>(y), n16,
+                                       reinterpret_cast<unsigned *>(static_cast<char *>(y) + n16 * 16), ntail);
+  check_launch();
+}
+
 template <class T>
 void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
   const size_t bytes = (size_t)t->n * k * sizeof(T);
   t->sfy.reserve(bytes);
   T *y = reinterpret_cast<T *>(t->sfy.p);
-  const size_t n16 = bytes / 16;
-  const int ntail = (int)((bytes - n16 * 16) / 4);
-  const int grid = (int)std::max<size_t>(1, std::min<size_t>(div_up(n16, (size_t)256), (size_t)num_sms() * 8));
-  k_fill_sentinel<<<grid, 256, 0, s>>>(reinterpret_cast<uint4 *>(y), n16,
-                                       reinterpret_cast<unsigned *>(reinterpret_cast<char *>(y) + n16 * 16), ntail);
-  check_launch();
+  fill_sentinel(y, bytes, s);
   if (t->arith == kArithFused) sf_ar<T, kArithFused>(t, x, y, k, s);
   else sf_ar<T, kArithExact>(t, x, y, k, s);
 }

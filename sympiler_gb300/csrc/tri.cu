@@ -675,7 +675,7 @@ extern "C" int gbsym_tri_get_info(gbsym_tri t, gbsym_tri_info *info) {
 
 extern "C" int gbsym_tri_set_exec(gbsym_tri t, int exec) {
   if (!t) return GBSYM_ERR_NULL_ARG;
-  if (exec < GBSYM_EXEC_AUTO || exec > GBSYM_EXEC_CLUSTER) return GBSYM_ERR_UNSUPPORTED;
+  if (exec < GBSYM_EXEC_AUTO || exec > GBSYM_EXEC_PARTITIONED) return GBSYM_ERR_UNSUPPORTED;
   t->exec_forced = exec;
   return GBSYM_OK;
 }

@@ -90,6 +90,12 @@ struct gbsym_tri_s {
   };
   std::vector<SfUnits> sf_units;
   int sf_blocks_per_sm = 0;          // sync-free grid (0: default)
+  struct PartPlan {
+    int R = 0, nparts = 0, ngroups = 0;  // rows per partition (0: not built)
+    gbsym::DBuf<int> part_group, group_ptr, rows;
+  };
+  PartPlan part;                     // partitioned executor's schedule
+  int part_rows_pref = 0;            // partition size (0: default)
   gbsym::DBuf<char> scratch;         // layout-conversion scratch
   gbsym::DBuf<char> io;              // device copy for host-memory solves
   cudaStream_t cap_stream = nullptr; // private stream for graph capture

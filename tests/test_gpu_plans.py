@@ -43,7 +43,7 @@ def test_c2_forward_multi_rhs_bit_exact(gpu, orc, c2_factor, k):
     assert np.array_equal(x.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("exec_mode", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("exec_mode", [1, 2, 3, 4, 5, 6])
 def test_executors_agree(gpu, orc, c2_factor, exec_mode):
     from sympiler_gb300.plans import TriPlan
     _, L, Lt = c2_factor
@@ -87,7 +87,7 @@ def test_multi_rhs_executors(gpu, orc, c2_factor, exec_mode, k):
     assert np.array_equal(x.cpu().numpy(), ref)
 
 
-@pytest.mark.parametrize("exec_mode", [1, 2, 4, 5])
+@pytest.mark.parametrize("exec_mode", [1, 2, 4, 5, 6])
 @pytest.mark.parametrize("k", [1, 8])
 def test_fused_arithmetic_within_tolerance(gpu, orc, c2_factor, exec_mode, k):
     """FUSED mode (one FMA per entry) stays within 1e-12 relative of the
@@ -109,12 +109,43 @@ def test_fused_arithmetic_within_tolerance(gpu, orc, c2_factor, exec_mode, k):
     assert rel < 1e-12, rel
 
 
+@pytest.mark.parametrize("rows", [64, 1000, 25600])
+def test_partitioned_executor_partition_sizes(gpu, orc, c2_factor, monkeypatch, rows):
+    """Contiguous partitions of 64 rows (many partitions per block), 1000
+    rows and 25,600 rows (levels wider than a block inside a partition),
+    forward and backward, FP64 and FP32 storage: the oracle's bits."""
+    from sympiler_gb300._lib import EXEC_PARTITIONED, UPPER_DIAG_FIRST
+    from sympiler_gb300.plans import TriPlan
+    monkeypatch.setenv("GBSYM_PART_ROWS", str(rows))
+    _, L, Lt = c2_factor
+    b = np.random.default_rng(rows).standard_normal(L.n)
+    for kind, M, solve in ((None, L, orc.sptrsv_csr), (UPPER_DIAG_FIRST, Lt, orc.ltsolve)):
+        ref = b.copy()
+        solve(L.n, *M.astuple(), ref)
+        plan = TriPlan(L.n, *M.astuple()) if kind is None else TriPlan(L.n, *M.astuple(), kind=kind)
+        plan.set_exec(EXEC_PARTITIONED)
+        x = torch.from_numpy(b.copy()).cuda()
+        for _ in range(2):
+            x.copy_(torch.from_numpy(b))
+            plan.solve(x)
+        plan.check()
+        assert np.array_equal(x.cpu().numpy(), ref)
+    ref32 = b.astype(np.float32)
+    orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), ref32)
+    p32 = TriPlan(L.n, *L.astuple(), dtype="f32")
+    p32.set_exec(EXEC_PARTITIONED)
+    x32 = torch.from_numpy(b.astype(np.float32)).cuda()
+    p32.solve(x32)
+    p32.check()
+    assert np.array_equal(x32.cpu().numpy(), ref32)
+
+
 def test_autotune_picks_a_working_executor(gpu, orc, c2_factor):
     from sympiler_gb300.plans import TriPlan
     _, L, _ = c2_factor
     plan = TriPlan(L.n, *L.astuple())
     chosen = plan.autotune(k=1)
-    assert chosen in (1, 2, 3, 4, 5)
+    assert chosen in (1, 2, 3, 4, 5, 6)
     b = np.random.default_rng(8).standard_normal(L.n)
     ref = b.copy()
     orc.sptrsv_csr(L.n, *L.astuple(), ref)
