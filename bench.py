@@ -552,10 +552,10 @@ def main():
         for arith_name, arith in (("exact", 0), ("fused", 1)):
             plan.set_arith(arith)
             for name, mode in (("levelset_graph_pdl", 1), ("syncfree", 2), ("persistent", 4), ("oneblock", 3),
-                               ("cluster", 5)):
+                               ("cluster", 5), ("partitioned", 6)):
                 key = "%s_%s" % (name, arith_name)
                 ex[key] = {"us_1rhs": time_exec(mode, x1w, x1)}
-                if mode != 3:
+                if mode not in (3, 6):  # one right-hand side only
                     ex[key]["us_%drhs" % k] = time_exec(mode, X, B)
         plan.set_arith(0)
         plan.set_exec(0)
@@ -564,6 +564,7 @@ def main():
         extras["executors"] = ex
         # IC0-PCG to 1e-10 on C2 (FP64 throughout)
         Pt = TriPlan(n, *Lt.astuple(), kind=UPPER_DIAG_FIRST)
+        Pt.autotune(k=1)
         Ac = CsrPlan(n, *A.astuple())
         xs = np.random.default_rng(7).standard_normal(n)
         bb = torch.from_numpy(A.scipy() @ xs).to(dev)
@@ -586,6 +587,7 @@ def main():
         for prec in ("f32", "f64"):
             Lu = TriPlan(C.n, dC[0], dC[1], lu, kind=ILU_UNIT_LOWER, diags=dC[3], dtype=prec)
             Up = TriPlan(C.n, dC[0], dC[1], lu, kind=ILU_UPPER, diags=dC[3], dtype=prec)
+            tuned_prec = [EXEC_NAMES.get(P.autotune(k=1, dtype=prec)) for P in (Lu, Up)]
             xg = torch.zeros(C.n, dtype=torch.float64, device=dev)
             plans.gmres(Cp, Lu, Up, bc, xg, mr=30, maxit=100, tol=1e-10)
             runs = []
@@ -594,7 +596,7 @@ def main():
                 runs.append(plans.gmres(Cp, Lu, Up, bc, xg, mr=30, maxit=100, tol=1e-10))
             best = min(runs, key=lambda r: r.seconds)
             out[prec] = {"seconds": best.seconds, "iterations": best.iterations, "restarts": best.restarts,
-                         "relres": best.relres, "status": best.status}
+                         "relres": best.relres, "status": best.status, "executors": tuned_prec}
         out["speedup_fp32_precond"] = out["f64"]["seconds"] / out["f32"]["seconds"]
         extras["gmres_c3"] = out
         del Cp, dC, lu
