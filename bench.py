@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--extras-only", action="store_true")
     ap.add_argument("--exec", default="auto",
-                    choices=["auto", "levelset", "syncfree", "oneblock", "persistent", "cluster"],
+                    choices=["auto", "levelset", "syncfree", "oneblock", "persistent", "cluster", "partitioned"],
                     help="force one executor instead of autotuning (profiling runs)")
     return ap.parse_args()
 
