@@ -66,6 +66,8 @@ void choose_exec(gbsym_tri_s *t) {
   if (const char *pb = std::getenv("GBSYM_PERSIST_BLOCKS")) t->persist_blocks = std::atoi(pb);
   if (const char *cb = std::getenv("GBSYM_CLUSTER_BLOCKS")) t->cluster_blocks = std::atoi(cb);
   if (const char *sb = std::getenv("GBSYM_SF_BLOCKS_PER_SM")) t->sf_blocks_per_sm = std::atoi(sb);
+  t->sf_deal = num_sms();
+  if (const char *sd = std::getenv("GBSYM_SF_DEAL")) t->sf_deal = std::atoi(sd);
 }
 
 template <class T>

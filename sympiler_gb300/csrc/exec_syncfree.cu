@@ -100,6 +100,21 @@ __device__ __forceinline__ bool all_ready(const T (&v)[VEC]) {
 __device__ __forceinline__ long long clock_now() { return clock64(); }
 constexpr long long kWaitLimitCycles = 1ll << 32;
 
+// Position of this warp in the order units are dealt.  A cooperative grid
+// of R blocks per SM over nsm SMs places blocks b and b + nsm on one SM (the
+// usual round-robin placement); dealing unit u to
+//   v = ((b / nsm) * warps_per_block + w) * nsm + b % nsm
+// puts consecutive units on consecutive SMs and then on different warp
+// slots of an SM, so a level's units spread evenly over SMs and their
+// sub-partitions instead of filling a contiguous range of blocks (which
+// gives some SMs twice the rows of others).  The map is a bijection of the
+// warps, so any placement stays correct.  nsm = 0 keeps the plain order.
+__device__ __forceinline__ int deal_warp(int nsm) {
+  const int wpb = blockDim.x >> 5, w = threadIdx.x >> 5, b = blockIdx.x;
+  if (nsm <= 0 || gridDim.x % nsm != 0) return b * wpb + w;
+  return ((b / nsm) * wpb + w) * nsm + b % nsm;
+}
+
 // G lanes per row; each lane owns the slices r = gl*VEC + s*G*VEC of its
 // row and works on one slice at a time.  Warp units hold rows of a single
 // level (units are cut per level), so no row of a unit waits on another.
@@ -110,12 +125,12 @@ constexpr long long kWaitLimitCycles = 1ll << 32;
 template <class T, int G, int VEC, int AR>
 __global__ void __launch_bounds__(kSfBlock)
 k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int *__restrict__ unit_row,
-           const int *__restrict__ unit_cnt, int nunits, int *err) {
+           const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int gl = lane % G;
   const int sub = lane / G;
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int warp = deal_warp(nsm);
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nslices = (k + G * VEC - 1) / (G * VEC);
   for (int u = warp; u < nunits; u += nwarps) {
@@ -247,18 +262,20 @@ static void sf_g(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   const bool v4 = sizeof(T) == 4 && (k % 4 == 0) && ((uintptr_t)x % 16 == 0);
   const bool v2 = (k % 2 == 0) && ((uintptr_t)x % (2 * sizeof(T)) == 0);
   if (v4)
-    launch_coop(t, k, k_syncfree<T, G, (sizeof(T) == 4 ? 4 : 2), AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->err.p);
+    launch_coop(t, k, k_syncfree<T, G, (sizeof(T) == 4 ? 4 : 2), AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal,
+                t->err.p);
   else if (v2)
-    launch_coop(t, k, k_syncfree<T, G, 2, AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->err.p);
+    launch_coop(t, k, k_syncfree<T, G, 2, AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
   else
-    launch_coop(t, k, k_syncfree<T, G, 1, AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->err.p);
+    launch_coop(t, k, k_syncfree<T, G, 1, AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
 }
 
 template <class T, int AR>
 static void sf_ar(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   if (k == 1) {
     const Units U = sf_units(t, 32);
-    launch_coop(t, k, k_syncfree<T, 1, 1, AR>, s, view_of<T>(t), x, y, 1, U.row, U.cnt, U.n, t->err.p);
+    launch_coop(t, k, k_syncfree<T, 1, 1, AR>, s, view_of<T>(t), x, y, 1, U.row, U.cnt, U.n, t->sf_deal,
+                t->err.p);
     return;
   }
   switch (lanes_for(k, sizeof(T))) {

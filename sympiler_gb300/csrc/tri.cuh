@@ -90,6 +90,7 @@ struct gbsym_tri_s {
   };
   std::vector<SfUnits> sf_units;
   int sf_blocks_per_sm = 0;          // sync-free grid (0: default)
+  int sf_deal = 0;                   // sync-free unit dealing: SM count to spread over (0: plain order)
   struct PartPlan {
     int R = 0, nparts = 0, ngroups = 0;  // rows per partition (0: not built)
     gbsym::DBuf<int> part_group, group_ptr, rows;
