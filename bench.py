@@ -153,6 +153,9 @@ def run_reference(args):
     import oracle
     from sympiler_gb300 import matgen as mg
     orc = oracle.orc()
+    # the reference's own executors where they were compiled from its
+    # sources (this needs the reference tree at build time), else the port
+    ref = oracle.ref()
     A = mg.lap3d(args.grid, 1e-2)
     U = mg.triu(A)
     f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
@@ -164,16 +167,26 @@ def run_reference(args):
     sample_cols = max(1, min(k, 8))
     B = rng.standard_normal((sample_cols, L.n))
 
+    from concurrent.futures import ThreadPoolExecutor
+    pool = ThreadPoolExecutor(max_workers=cores)
+
     def t_levelset():
         X = B.copy()
         t0 = time.perf_counter()
-        orc.sptrsv_csr_levelset_mrhs(L.n, *L.astuple(), X, sample_cols, nl, lp, ls, cores)
+        if ref is not None:  # one OpenMP level-set solve per column, as the reference runs it
+            for c in range(sample_cols):
+                ref.sptrsv_csr_levelset(L.n, *L.astuple(), X[c], nl, lp, ls)
+        else:
+            orc.sptrsv_csr_levelset_mrhs(L.n, *L.astuple(), X, sample_cols, nl, lp, ls, cores)
         return (time.perf_counter() - t0) * k / sample_cols
 
     def t_colpar():
         X = B.copy()
         t0 = time.perf_counter()
-        orc.sptrsv_csr_mrhs(L.n, *L.astuple(), X, sample_cols, cores)
+        if ref is not None:  # serial sptrsv_csr per column, columns over host threads
+            list(pool.map(lambda c: ref.sptrsv_csr(L.n, *L.astuple(), X[c]), range(sample_cols)))
+        else:
+            orc.sptrsv_csr_mrhs(L.n, *L.astuple(), X, sample_cols, cores)
         # columns run in parallel: a sample of c columns on >= c threads
         # takes one column's time; k columns take ceil(k / threads) rounds
         dt = time.perf_counter() - t0
@@ -190,13 +203,14 @@ def run_reference(args):
     byt = algorithmic_bytes(L.nnz, L.n, k)
     tl, tc = statistics.median(ts_l), statistics.median(ts_c)
     best, kind = (tl, "sptrsv_csr_levelset, OpenMP per level") if tl <= tc else \
-        (tc, "sptrsv_csr per column, columns over OpenMP threads")
+        (tc, "sptrsv_csr per column, columns over %s threads" % ("host" if ref is not None else "OpenMP"))
     value = byt / best / 1e9
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": best * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config(args.grid, k),
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores,
+                             "kind": "reference" if ref is not None else "port",
                              "sample": "%d of %d RHS columns per step, scaled to %d; best of: levelset "
                                        "%.1f ms, column-parallel %.1f ms per %d-RHS solve; used: %s"
                                        % (sample_cols, k, k, tl * 1e3, tc * 1e3, k, kind)},
