@@ -140,6 +140,55 @@ def test_partitioned_executor_partition_sizes(gpu, orc, c2_factor, monkeypatch, 
     assert np.array_equal(x32.cpu().numpy(), ref32)
 
 
+def _long_rows_lower(n=3000, seed=21):
+    """Lower triangle whose rows hold 0 to ~60 off-diagonals, plus a few rows
+    with hundreds: every executor's overflow path (entries past the 8-slot
+    slab) runs.  Off-diagonals are scaled by the row length so the solution
+    stays bounded."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    m = sp.random(n, n, density=0.02, format="coo", random_state=rng)
+    low = m.row > m.col
+    r, c = list(m.row[low]), list(m.col[low])
+    for i in (n - 7, n - 5, n - 2):  # near-dense rows
+        cols = np.arange(0, i, 7)
+        r += [i] * len(cols)
+        c += list(cols)
+    r, c = np.array(r), np.array(c)
+    M = sp.coo_matrix((np.ones(len(r)), (r, c)), shape=(n, n)).tocsr()
+    M.data[:] = 1.0  # duplicates summed above
+    lens = np.diff(M.indptr)
+    M.data = rng.uniform(-1.0, 1.0, M.nnz) / (1.0 + np.repeat(lens, lens))
+    D = sp.diags(1.0 + rng.uniform(0.0, 1.0, n))
+    return mg.from_scipy(M + D)
+
+
+@pytest.mark.parametrize("exec_mode", [1, 2, 3, 4, 5, 6])
+def test_long_rows_every_executor(gpu, orc, exec_mode):
+    from sympiler_gb300.plans import TriPlan
+    L = _long_rows_lower()
+    assert np.diff(L.p).max() > 100
+    plan = TriPlan(L.n, *L.astuple())
+    plan.set_exec(exec_mode)
+    p32 = TriPlan(L.n, *L.astuple(), dtype="f32")
+    p32.set_exec(exec_mode)
+    rng = np.random.default_rng(exec_mode)
+    for k in (1, 5, 64):
+        B = rng.standard_normal((L.n, k))
+        ref = _oracle_mrhs(orc, L, B)
+        x = torch.from_numpy(B.copy()).cuda()
+        plan.solve(x if k > 1 else x.view(-1))
+        plan.check()
+        assert np.array_equal(x.cpu().numpy(), ref), k
+    b32 = rng.standard_normal(L.n).astype(np.float32)
+    ref32 = b32.copy()
+    orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), ref32)
+    x32 = torch.from_numpy(b32.copy()).cuda()
+    p32.solve(x32)
+    p32.check()
+    assert np.array_equal(x32.cpu().numpy(), ref32)
+
+
 def test_autotune_picks_a_working_executor(gpu, orc, c2_factor):
     from sympiler_gb300.plans import TriPlan
     _, L, _ = c2_factor
