@@ -295,6 +295,34 @@ def bench_batch(dev, stream, flush, nsys=512, k=8):
     return res
 
 
+def bench_spmv(dev, stream, flush):
+    """CSR SpMV y = A x (the Krylov drivers' system product) on the C3 and C2
+    operators, FP64, L2 flushed before every timed call.  Bytes are the
+    survey's B_spmv = (V + 4) nnz + 4 (n + 1) + 2 S n."""
+    import torch
+    from sympiler_gb300 import matgen as mg
+    from sympiler_gb300.plans import CsrPlan
+    peak = 6800.0
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peak = json.load(fh).get("hbm_gbs") or peak
+    except (OSError, ValueError):
+        pass
+    out = {}
+    for name, A in (("c3_convdiff_96", mg.convdiff3d(96)), ("c2_lap3d_64", mg.lap3d(64, 1e-2))):
+        P = CsrPlan(A.n, *A.astuple())
+        x = torch.from_numpy(np.random.default_rng(3).uniform(-1, 1, A.n)).to(dev)
+        y = torch.empty_like(x)
+        P.spmv(x, y)
+        t = _time(lambda: P.spmv(x, y), 10, stream, flush)
+        byt = 12 * A.nnz + 4 * (A.n + 1) + 16 * A.n
+        out[name] = {"n": A.n, "nnz": int(A.nnz), "us": t * 1e6, "gbs": byt / t / 1e9,
+                     "hbm_frac": byt / t / 1e9 / peak,
+                     "fp64_gops": 2 * A.nnz / t / 1e9, "fp64_frac": 2 * A.nnz / t / 1e9 / FP64_PEAK_GOPS}
+        del P
+    return out
+
+
 def bench_adjoint(dev, stream, flush, g=1024, k=32):
     """Forward X = L^{-1} B and the reverse pass (L^T solve + value gradient)
     on the IC0 factor of the 1024^2 anisotropic variable-coefficient Poisson
@@ -616,6 +644,7 @@ def main():
         del Cp, dC, lu
         extras["batch_c4"] = bench_batch(dev, stream, flush)
         extras["adjoint_c5"] = bench_adjoint(dev, stream, flush)
+        extras["spmv"] = bench_spmv(dev, stream, flush)
         result["extras"] = extras
     if rank == 0:
         if not args.extras_only:

