@@ -2,11 +2,9 @@
 //
 // Reference: spmv_csr / spmv_csr_parallel (sparse_blas/spmv.cpp:12-21,
 // 37-57) and the accumulate form spmv_csr(..., y, z, a, b) (spmv.cpp:
-// 23-34).  A thread block owns kSpmvRows consecutive rows; their (column,
-// value) entries are one contiguous range of the CSR arrays, staged through
-// shared memory in chunks with coalesced loads.  Each row is then summed by
-// one thread in storage order with separately rounded multiply and add, the
-// order the reference uses, so FP64 results match it bit for bit.
+// 23-34).  Each row is summed by one thread in storage order with
+// separately rounded multiply and add, the order the reference uses, so
+// FP64 results match it bit for bit.
 #include <algorithm>
 #include <memory>
 
@@ -15,7 +13,6 @@
 namespace gbsym {
 
 constexpr int kSpmvRows = 256;
-constexpr int kSpmvChunk = 2048;
 
 // acc + RN(v * x), both roundings separate (the reference's order), issued
 // in FP64 as fused multiply-adds: RN(v*x) = fma(v, x, -0) and
@@ -32,41 +29,22 @@ __device__ __forceinline__ double madd_exact(double acc, double v, double x) {
 __device__ __forceinline__ float madd_exact(float acc, float v, float x) { return add_rn(acc, mul_rn(v, x)); }
 
 // MODE 0: y = A x.  MODE 1: z = alpha (z + A x) + beta y.
+// One thread per row, loading its entries directly: on this part the
+// exact FP64 sum is bound by FP64 issue (two FMAs per entry), so the kernel
+// keeps many independent rows in flight with no block barrier in the way;
+// this measured 5-10% faster than staging each block's entries through
+// shared memory.
 template <class T, int MODE>
 __global__ void __launch_bounds__(kSpmvRows)
 k_spmv(int n, const int *__restrict__ p, const int *__restrict__ ci, const T *__restrict__ val,
        const T *__restrict__ x, const T *__restrict__ yin, T *__restrict__ out, T alpha, T beta) {
-  __shared__ int s_ci[kSpmvChunk];
-  __shared__ T s_v[kSpmvChunk];
-  const int r0 = blockIdx.x * kSpmvRows;
-  const int r1 = min(r0 + kSpmvRows, n);
-  const int row = r0 + threadIdx.x;
-  const bool active = row < r1;
-  const int e0 = p[r0], e1 = p[r1];
-  int lo = 0, hi = 0;
-  T acc = T(0);
-  if (active) {
-    lo = p[row];
-    hi = p[row + 1];
-    if (MODE == 1) acc = out[row];
-  }
-  for (int c0 = e0; c0 < e1; c0 += kSpmvChunk) {
-    const int c1 = min(c0 + kSpmvChunk, e1);
-    if (c0 != e0) __syncthreads();
-    for (int e = c0 + threadIdx.x; e < c1; e += kSpmvRows) {
-      s_ci[e - c0] = ci[e];
-      s_v[e - c0] = val[e];
-    }
-    __syncthreads();
-    if (active) {
-      const int a = max(lo, c0), z = min(hi, c1);
-      for (int e = a; e < z; ++e) acc = madd_exact(acc, s_v[e - c0], x[s_ci[e - c0]]);
-    }
-  }
-  if (active) {
-    if (MODE == 1) acc = add_rn(mul_rn(alpha, acc), mul_rn(beta, yin[row]));
-    out[row] = acc;
-  }
+  const int row = blockIdx.x * kSpmvRows + threadIdx.x;
+  if (row >= n) return;
+  const int lo = p[row], hi = p[row + 1];
+  T acc = MODE == 1 ? out[row] : T(0);
+  for (int e = lo; e < hi; ++e) acc = madd_exact(acc, val[e], x[ci[e]]);
+  if (MODE == 1) acc = add_rn(mul_rn(alpha, acc), mul_rn(beta, yin[row]));
+  out[row] = acc;
 }
 
 template <class T>
