@@ -21,6 +21,7 @@
 // chain.  Waits are bounded: a lane that sees no progress for the wait
 // limit records GBSYM_ERR_TIMEOUT and every warp leaves the sweep.
 #include <algorithm>
+#include <cstdlib>
 #include <vector>
 
 #include "exec_common.cuh"
@@ -273,9 +274,12 @@ static void sf_g(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
 template <class T, int AR>
 static void sf_ar(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   if (k == 1) {
-    const Units U = sf_units(t, 32);
-    launch_coop(t, k, k_syncfree<T, 1, 1, AR>, s, view_of<T>(t), x, y, 1, U.row, U.cnt, U.n, t->sf_deal,
-                t->err.p);
+    // one right-hand side: 8 rows per warp unit (4 lanes each, one active).
+    // A unit waits for all its rows' dependencies before computing, so
+    // fewer rows per unit shorten that wait; fewer than 8 costs more in
+    // FP64 issue slots than it saves (measured on the C2 and C3 factors:
+    // 8 rows 4-5% faster than 32, 1 row twice as slow)
+    sf_g<T, 4, AR>(t, x, y, k, s);
     return;
   }
   switch (lanes_for(k, sizeof(T))) {
