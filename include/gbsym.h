@@ -192,6 +192,90 @@ int gbsym_build_lbc(int n, const int *Lp, const int *Li, const double *cost,
  * pattern of the CSR (Lp, Li): parent[n], -1 at roots. */
 int gbsym_etree_lower_csr(int n, const int *Lp, const int *Li, int *parent);
 
+/* ---- supernodal (blocked CSC) solves ----------------------------------- */
+/* Storage of the reference's ParSy blocked solves: supernode s owns columns
+ * sup2col[s] .. sup2col[s+1]-1 (sup2col has supNo+1 entries, 0 .. n); its
+ * rows are Li[Li_ptr[c0] .. Li_ptr[c1]), its own columns first, then the
+ * rows below it ascending; its values are a column-major block of
+ * Li_ptr[c1] - Li_ptr[c0] rows at Lx + Lp[c0] (only the lower triangle of
+ * the diagonal block is read).  Lp and Li_ptr have n+1 size_t entries.  NNZ
+ * and col2sup are accepted and unused (the reference's blocked solves do not
+ * read them either).  x is host memory, column-major n x rhs, solved in
+ * place; the functions return 1 on success and 0 otherwise (the status is
+ * in gbsym_last_error()), as the reference's return 1/0.
+ *
+ * Forward: the reference's order, bit for bit (its dense kernels'
+ * groupings).  Replaces parsy::blockedLsolve
+ * (sparse_blas/parsy/triangularSolve/Triangular_BCSC.cpp:23-58). */
+int gbsym_parsy_blockedLsolve(int n, size_t *Lp, int *Li, double *Lx, int NNZ,
+                              size_t *Li_ptr, int *col2sup, int *sup2col,
+                              int supNo, double *x);
+/* Replaces parsy::blockedLsolve_mrhs (Triangular_BCSC.cpp:62-121): each of
+ * the n_rhs columns as blockedLsolve solves it; max_col is unused. */
+int gbsym_parsy_blockedLsolve_mrhs(int n, size_t *Lp, int *Li, double *Lx,
+                                   int NNZ, size_t *Li_ptr, int *col2sup,
+                                   int *sup2col, int supNo, double *x,
+                                   int n_rhs, int max_col);
+/* Replaces parsy::leveledBlockedLsolve (Triangular_BCSC.cpp:401-449): the
+ * level set over supernodes is validated; the result equals blockedLsolve's
+ * (the reference's atomic updates make its own order vary). */
+int gbsym_parsy_leveledBlockedLsolve(int n, size_t *Lp, int *Li, double *Lx,
+                                     int NNZ, size_t *Li_ptr, int *col2sup,
+                                     int *sup2col, int supNo, double *x,
+                                     int levels, int *levelPtr, int *levelSet,
+                                     int chunk);
+/* Replaces parsy::H2LeveledBlockedLsolve (Triangular_BCSC.cpp:512-581) and
+ * its _mrhs form: the LBC schedule over supernodes (levelPtr -> parPtr ->
+ * partition) is validated; results as blockedLsolve's. */
+int gbsym_parsy_H2LeveledBlockedLsolve(int n, size_t *Lp, int *Li, double *Lx,
+                                       int NNZ, size_t *Li_ptr, int *col2sup,
+                                       int *sup2col, int supNo, double *x,
+                                       int levels, int *levelPtr,
+                                       int *levelSet, int parts, int *parPtr,
+                                       int *partition, int chunk);
+int gbsym_parsy_H2LeveledBlockedLsolve_mrhs(
+    int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr,
+    int *col2sup, int *sup2col, int supNo, double *x, int n_rhs, int levels,
+    int *levelPtr, int *levelSet, int parts, int *parPtr, int *partition,
+    int chunk, int max_col);
+/* Transposed solve L^T x = b.  Replaces parsy::blockedLTsolve
+ * (Triangular_BCSC.cpp:124-184), its _mrhs form and
+ * H2LeveledBlockedLTsolve(_mrhs).  The reference computes this with an
+ * external BLAS (dgemv/dtrsm, summation order the library's) or, in its
+ * SYM_BLAS build, with the forward kernels (marked FIXME there); here each
+ * supernode column subtracts its off-block rows' products in storage order,
+ * then the diagonal block's transpose is solved backward. */
+int gbsym_parsy_blockedLTsolve(int n, size_t *Lp, int *Li, double *Lx, int NNZ,
+                               size_t *Li_ptr, int *col2sup, int *sup2col,
+                               int supNo, double *x);
+int gbsym_parsy_blockedLTsolve_mrhs(int n, size_t *Lp, int *Li, double *Lx,
+                                    int NNZ, size_t *Li_ptr, int *col2sup,
+                                    int *sup2col, int supNo, double *x,
+                                    int m_rhs, int max_col);
+int gbsym_parsy_H2LeveledBlockedLTsolve(int n, size_t *Lp, int *Li, double *Lx,
+                                        int NNZ, size_t *Li_ptr, int *col2sup,
+                                        int *sup2col, int supNo, double *x,
+                                        int levels, int *levelPtr,
+                                        int *levelSet, int parts, int *parPtr,
+                                        int *partition, int chunk);
+int gbsym_parsy_H2LeveledBlockedLTsolve_mrhs(
+    int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr,
+    int *col2sup, int *sup2col, int supNo, double *x, int m_rhs, int levels,
+    int *levelPtr, int *levelSet, int parts, int *parPtr, int *partition,
+    int chunk, int max_col);
+
+/* Supernodal plan: the factor resident on the GPU with its supernode level
+ * schedules (host arrays in).  gbsym_sn_solve works on device memory, x
+ * column-major n x k, forward (transposed = 0) or L^T (transposed = 1);
+ * stream-ordered.  A supernode may be at most 5120 columns wide. */
+typedef struct gbsym_sn_s *gbsym_sn;
+int gbsym_sn_create(gbsym_sn *out, int n, const size_t *Lp, const int *Li,
+                    const double *Lx, const size_t *Li_ptr, const int *sup2col,
+                    int supNo, void *stream);
+int gbsym_sn_destroy(gbsym_sn t);
+int gbsym_sn_levels(gbsym_sn t, int *forward_levels, int *transposed_levels);
+int gbsym_sn_solve(gbsym_sn t, double *x, int k, int transposed, void *stream);
+
 /* ======================================================================== */
 /* Plans (device-resident).                                                 */
 /* ======================================================================== */

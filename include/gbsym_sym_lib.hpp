@@ -177,6 +177,57 @@ inline int lsolveParH2(int n, int *Lp, int *Li, double *Lx, double *x, int level
   return gbsym_parsy_lsolveParH2(n, Lp, Li, Lx, x, levels, levelPtr, levelSet, parts, parPtr,
                                  partition, chunk);
 }
+// Triangular_BCSC.h: supernodal (blocked CSC) solves
+inline int blockedLsolve(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr, int *col2sup,
+                         int *sup2col, int supNo, double *x) {
+  return gbsym_parsy_blockedLsolve(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x);
+}
+inline int blockedLsolve_mrhs(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr, int *col2sup,
+                              int *sup2col, int supNo, double *x, int n_rhs, int max_col = -1) {
+  return gbsym_parsy_blockedLsolve_mrhs(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x, n_rhs, max_col);
+}
+inline int blockedLTsolve(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr, int *col2sup,
+                          int *sup2col, int supNo, double *x) {
+  return gbsym_parsy_blockedLTsolve(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x);
+}
+inline int blockedLTsolve_mrhs(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr, int *col2sup,
+                               int *sup2col, int supNo, double *x, int m_rhs, int max_col = -1) {
+  return gbsym_parsy_blockedLTsolve_mrhs(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x, m_rhs, max_col);
+}
+inline int leveledBlockedLsolve(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr, int *col2sup,
+                                int *sup2col, int supNo, double *x, int levels, int *levelPtr, int *levelSet,
+                                int chunk) {
+  return gbsym_parsy_leveledBlockedLsolve(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x, levels,
+                                          levelPtr, levelSet, chunk);
+}
+inline int H2LeveledBlockedLsolve(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr, int *col2sup,
+                                  int *sup2col, int supNo, double *x, int levels, int *levelPtr, int *levelSet,
+                                  int parts, int *parPtr, int *partition, int chunk) {
+  return gbsym_parsy_H2LeveledBlockedLsolve(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x, levels,
+                                            levelPtr, levelSet, parts, parPtr, partition, chunk);
+}
+inline int H2LeveledBlockedLTsolve(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr, int *col2sup,
+                                   int *sup2col, int supNo, double *x, int levels, int *levelPtr, int *levelSet,
+                                   int parts, int *parPtr, int *partition, int chunk) {
+  return gbsym_parsy_H2LeveledBlockedLTsolve(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x, levels,
+                                             levelPtr, levelSet, parts, parPtr, partition, chunk);
+}
+inline int H2LeveledBlockedLsolve_mrhs(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr,
+                                       int *col2sup, int *sup2col, int supNo, double *x, int n_rhs, int levels,
+                                       int *levelPtr, int *levelSet, int parts, int *parPtr, int *partition,
+                                       int chunk, int max_col = -1) {
+  return gbsym_parsy_H2LeveledBlockedLsolve_mrhs(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x, n_rhs,
+                                                 levels, levelPtr, levelSet, parts, parPtr, partition, chunk,
+                                                 max_col);
+}
+inline int H2LeveledBlockedLTsolve_mrhs(int n, size_t *Lp, int *Li, double *Lx, int NNZ, size_t *Li_ptr,
+                                        int *col2sup, int *sup2col, int supNo, double *x, int m_rhs, int levels,
+                                        int *levelPtr, int *levelSet, int parts, int *parPtr, int *partition,
+                                        int chunk, int max_col = -1) {
+  return gbsym_parsy_H2LeveledBlockedLTsolve_mrhs(n, Lp, Li, Lx, NNZ, Li_ptr, col2sup, sup2col, supNo, x, m_rhs,
+                                                  levels, levelPtr, levelSet, parts, parPtr, partition, chunk,
+                                                  max_col);
+}
 // mgmres.hpp:41
 inline void lus_cr(int n, int nz_num, int ia[], int ja[], double l[], int ua[], double r[],
                    double z[]) {

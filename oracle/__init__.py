@@ -20,6 +20,7 @@ from . import build as _build
 
 _i = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
 _d = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_z = np.ctypeslib.ndpointer(dtype=np.uint64, flags="C_CONTIGUOUS")  # size_t arrays
 _f = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 _int, _dbl, _vp = C.c_int, C.c_double, C.c_void_p
 
@@ -73,6 +74,17 @@ class _Orc:
                                              _dbl, _int, C.POINTER(_dbl)])
         self._gmres = b("orc_gmres_ilu0", _int, [_int, _i, _i, _d, _d, _i, _d, _d, _int, _int,
                                                   _dbl, C.POINTER(_dbl)])
+        self._blk_l = b("orc_blocked_lsolve", None, [_int, _z, _i, _d, _z, _i, _int, _d, _int])
+        self._blk_lt = b("orc_blocked_ltsolve", None, [_int, _z, _i, _d, _z, _i, _int, _d, _int])
+
+    def blocked_lsolve(self, S, X):
+        """Supernodal forward solve; X is (nrhs, n) C-contiguous = column-major n x nrhs."""
+        nrhs = 1 if X.ndim == 1 else X.shape[0]
+        self._blk_l(S.n, S.Lp, S.Li, S.Lx, S.Li_ptr, S.sup2col, S.nsup, X, nrhs)
+
+    def blocked_ltsolve(self, S, X):
+        nrhs = 1 if X.ndim == 1 else X.shape[0]
+        self._blk_lt(S.n, S.Lp, S.Li, S.Lx, S.Li_ptr, S.sup2col, S.nsup, X, nrhs)
 
     # ---- convenience wrappers returning numpy arrays ----------------------
     def sptrsv_csr_levelset(self, n, Lp, Li, Lx, x, levels, lp, ls, nthreads=1):
@@ -174,6 +186,22 @@ class _Ref:
         self._tree_lvl = b("ref_tree_levelset", _int, [_int, _i, _i, _i])
         self._coarse6 = b("ref_coarse_levelset6", _int,
                           [_int, _i, _int, _int, _int, _d, _i, _i, _i, C.POINTER(_int)])
+        self._blk_l = b("ref_blocked_lsolve", _int, [_int, _z, _i, _d, _z, _i, _i, _int, _d])
+        self._blk_l_lvl = b("ref_leveled_blocked_lsolve", _int,
+                            [_int, _z, _i, _d, _z, _i, _i, _int, _d, _int, _i, _i])
+        self._blk_l_h2 = b("ref_h2_leveled_blocked_lsolve", _int,
+                           [_int, _z, _i, _d, _z, _i, _i, _int, _d, _int, _i, _i, _int, _i, _i])
+
+    def blocked_lsolve(self, S, x):
+        return self._blk_l(S.n, S.Lp, S.Li, S.Lx, S.Li_ptr, S.col2sup, S.sup2col, S.nsup, x)
+
+    def leveled_blocked_lsolve(self, S, x, levels, lp, ls):
+        return self._blk_l_lvl(S.n, S.Lp, S.Li, S.Lx, S.Li_ptr, S.col2sup, S.sup2col, S.nsup, x,
+                               levels, lp, ls)
+
+    def h2_leveled_blocked_lsolve(self, S, x, levels, lp, ls, parts, pp, part):
+        return self._blk_l_h2(S.n, S.Lp, S.Li, S.Lx, S.Li_ptr, S.col2sup, S.sup2col, S.nsup, x,
+                              levels, lp, ls, parts, pp, part)
 
     def sptrsv_csr_lbc_redundant(self, n, Lp, Li, Lx, x, b, level_no, lp, pp, part, nthreads=64):
         tmp = np.zeros(n * nthreads, dtype=np.float64)

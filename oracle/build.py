@@ -46,7 +46,19 @@ REF_SOURCES = [
     "sparse_blas/parsy/symbolic/PostOrderSpliting.cpp",
     "sparse_blas/parsy/matrixVector/spmv_CSC.cpp",
     "sparse_blas/parsy/gmres/mgmres.cpp",
+    "sparse_blas/parsy/triangularSolve/Triangular_BCSC.cpp",
+    "sparse_blas/parsy/triangularSolve/BLAS.cpp",
 ]
+
+# The supernodal solves are built with the reference's own dense kernels
+# (SYM_BLAS); the external-BLAS calls of their other forms are routed to an
+# aborting stub declared by ref_shim/missing_blas.h.
+EXTRA_FLAGS = {
+    "sparse_blas/parsy/triangularSolve/Triangular_BCSC.cpp": [
+        "-DSYM_BLAS", "-DSYM_DTRSM=ref_blas_missing", "-DSYM_DGEMM=ref_blas_missing",
+        "-DSYM_DGEMV=ref_blas_missing", "-DSET_BLAS_THREAD(t)=((void)(t))",
+        "-include", os.path.join(HERE, "ref_shim", "missing_blas.h")],
+}
 
 FLAGS = ["-O3", "-fopenmp", "-fPIC", "-ffp-contract=off"]
 
@@ -85,18 +97,20 @@ def build_reference(reference_root: str | None = None, force: bool = False):
     os.makedirs(REF_DIR, exist_ok=True)
     capi = os.path.join(HERE, "ref_capi.cpp")
     shim = os.path.join(HERE, "ref_shim", "aggregation", "def.h")
+    blas_shim = os.path.join(HERE, "ref_shim", "missing_blas.h")
     srcs = [os.path.join(root, s) for s in REF_SOURCES]
-    if not (force or _stale(REF_SO, srcs + [capi, shim, __file__])):
+    if not (force or _stale(REF_SO, srcs + [capi, shim, blas_shim, __file__])):
         return REF_SO
     inc = ["-I" + os.path.join(HERE, "ref_shim"), "-I" + os.path.join(root, "include"),
            "-I" + os.path.join(root, "include", "sympiler"),
            "-I" + os.path.join(root, "include", "sympiler", "parsy")]
     objs = []
     jobs = []
-    for s in srcs + [capi]:
-        o = os.path.join(REF_DIR, os.path.basename(s).replace(".cpp", ".o"))
+    for s, rel in list(zip(srcs, REF_SOURCES)) + [(capi, None)]:
+        o = os.path.join(REF_DIR, (rel or "ref_capi.cpp").replace("/", "_").replace(".cpp", ".o"))
         objs.append(o)
-        jobs.append(["g++", "-std=c++11", "-DENABLE_OPENMP", *FLAGS, *inc, "-c", s, "-o", o])
+        jobs.append(["g++", "-std=c++11", "-DENABLE_OPENMP", *FLAGS, *EXTRA_FLAGS.get(rel, []), *inc,
+                     "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 1)) as ex:
         list(ex.map(_run, jobs))
     _run(["g++", "-shared", "-fopenmp", *objs, "-o", REF_SO, "-Wl,--no-undefined", "-lm"])

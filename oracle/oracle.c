@@ -583,3 +583,114 @@ int orc_gmres_ilu0(int n, const int *Ap, const int *Ai, const double *Ax,
   free(r); free(w); free(v); free(h); free(c); free(s); free(g); free(y);
   return itr_used;
 }
+
+/* ---- supernodal (blocked CSC) solves -------------------------------------- */
+
+/* Dense lower solve of the w x w diagonal block M (column-major, leading
+ * dimension ld) in place on rhs, with the reference's grouping: columns in
+ * runs of 8 while at least 8 remain past the current one, then runs of 4,
+ * then at most one run of 2 and one single column.  Inside a run each
+ * unknown subtracts the run's earlier unknowns left to right and divides;
+ * then every later row subtracts the run's products left to right
+ * (sparse_blas/parsy/triangularSolve/BLAS.cpp:12-106). */
+static void blk_diag_solve(int ld, int w, const double *M, double *rhs) {
+  int fc = 0;
+  for (;;) {
+    int g;
+    if (fc < w - 7) g = 8;
+    else if (fc < w - 3) g = 4;
+    else if (fc < w - 1) g = 2;
+    else if (fc == w - 1) g = 1;
+    else break;
+    double xg[8];
+    for (int a = 0; a < g; ++a) {
+      double v = rhs[fc + a];
+      for (int b = 0; b < a; ++b) v = v - xg[b] * M[(size_t)(fc + b) * ld + fc + a];
+      xg[a] = v / M[(size_t)(fc + a) * ld + fc + a];
+    }
+    for (int a = 0; a < g; ++a) rhs[fc + a] = xg[a];
+    for (int k = fc + g; k < w; ++k) {
+      double v = rhs[k];
+      for (int b = 0; b < g; ++b) v = v - xg[b] * M[(size_t)(fc + b) * ld + k];
+      rhs[k] = v;
+    }
+    fc += g;
+    if (g <= 2) {
+      /* after a run of 2 only a single column can remain, and after the
+         single column nothing */
+      if (g == 2 && fc == w - 1) continue;
+      break;
+    }
+  }
+}
+
+/* out[k] = dot of row k of the nrow x ncol block M (leading dimension ld)
+ * with vec, in the reference's grouping: column runs of 8, then 4, then 1;
+ * each run's products summed left to right, then added to the running
+ * value, which starts at +0 (BLAS.cpp:123-185). */
+static double blk_row_dot(int ld, int ncol, const double *M, int k, const double *vec) {
+  double acc = 0.0;
+  int fc = 0;
+  while (fc < ncol - 7) {
+    double s = vec[fc] * M[(size_t)fc * ld + k];
+    for (int b = 1; b < 8; ++b) s = s + vec[fc + b] * M[(size_t)(fc + b) * ld + k];
+    acc = acc + s;
+    fc += 8;
+  }
+  while (fc < ncol - 3) {
+    double s = vec[fc] * M[(size_t)fc * ld + k];
+    for (int b = 1; b < 4; ++b) s = s + vec[fc + b] * M[(size_t)(fc + b) * ld + k];
+    acc = acc + s;
+    fc += 4;
+  }
+  while (fc < ncol) {
+    acc = acc + vec[fc] * M[(size_t)fc * ld + k];
+    fc += 1;
+  }
+  return acc;
+}
+
+/* Triangular_BCSC.cpp:23-58: per supernode in increasing order, the dense
+ * diagonal solve, then the off-block product subtracted from the rows it
+ * reaches. */
+void orc_blocked_lsolve(int n, const size_t *Lp, const int *Li, const double *Lx,
+                        const size_t *Li_ptr, const int *sup2col, int supNo,
+                        double *x, int nrhs) {
+  for (int j = 0; j < nrhs; ++j) {
+    double *xj = x + (size_t)j * n;
+    for (int s = 0; s < supNo; ++s) {
+      const int c0 = sup2col[s], c1 = sup2col[s + 1], w = c1 - c0;
+      const int nr = (int)(Li_ptr[c1] - Li_ptr[c0]);
+      const double *M = Lx + Lp[c0];
+      blk_diag_solve(nr, w, M, xj + c0);
+      for (int k = w; k < nr; ++k) {
+        const double c = blk_row_dot(nr, w, M, k, xj + c0);
+        const int r = Li[Li_ptr[c0] + k];
+        xj[r] = xj[r] - c;
+      }
+    }
+  }
+}
+
+void orc_blocked_ltsolve(int n, const size_t *Lp, const int *Li, const double *Lx,
+                         const size_t *Li_ptr, const int *sup2col, int supNo,
+                         double *x, int nrhs) {
+  for (int j = 0; j < nrhs; ++j) {
+    double *xj = x + (size_t)j * n;
+    for (int s = supNo - 1; s >= 0; --s) {
+      const int c0 = sup2col[s], c1 = sup2col[s + 1], w = c1 - c0;
+      const int nr = (int)(Li_ptr[c1] - Li_ptr[c0]);
+      const double *M = Lx + Lp[c0];
+      for (int q = 0; q < w; ++q) {
+        double v = xj[c0 + q];
+        for (int k = w; k < nr; ++k) v = v - M[(size_t)q * nr + k] * xj[Li[Li_ptr[c0] + k]];
+        xj[c0 + q] = v;
+      }
+      for (int q = w - 1; q >= 0; --q) {
+        const double v = xj[c0 + q] / M[(size_t)q * nr + q];
+        xj[c0 + q] = v;
+        for (int i = 0; i < q; ++i) xj[c0 + i] = xj[c0 + i] - M[(size_t)i * nr + q] * v;
+      }
+    }
+  }
+}

@@ -16,6 +16,8 @@
 #ifndef GBSYM_ORACLE_H
 #define GBSYM_ORACLE_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -107,6 +109,29 @@ int orc_pcg_ic0(int n, const int *Ap, const int *Ai, const double *Ax,
 int orc_gmres_ilu0(int n, const int *Ap, const int *Ai, const double *Ax,
                    const double *lu, const int *ua, const double *b, double *x,
                    int mr, int itr_max, double tol_rel, double *relres);
+
+/* ---- supernodal (blocked CSC) solves ----------------------------------- */
+/* Supernode s owns columns sup2col[s] .. sup2col[s+1]-1; its rows are
+ * Li[Li_ptr[c0] .. Li_ptr[c1]) (the diagonal block's rows first) and its
+ * values a column-major block of nSupR rows at Lx + Lp[c0].  x is n x nrhs,
+ * column-major (leading dimension n).
+ *
+ * Forward solve in the order of parsy::blockedLsolve
+ * (sparse_blas/parsy/triangularSolve/Triangular_BCSC.cpp:23-58) with its
+ * dense kernels dlsolve_blas_nonUnit and dmatvec_blas
+ * (sparse_blas/parsy/triangularSolve/BLAS.cpp:12-121, 123-185), column by
+ * column. */
+void orc_blocked_lsolve(int n, const size_t *Lp, const int *Li, const double *Lx,
+                        const size_t *Li_ptr, const int *sup2col, int supNo,
+                        double *x, int nrhs);
+/* Transposed (backward) solve L^T x = b on the same storage: supernodes in
+ * decreasing order; per supernode column j, x_j -= sum over the off-block
+ * rows r (storage order) of L[r, j] x_r, each product and difference
+ * rounded; then the diagonal block's transpose backward, column j from the
+ * last: x_j /= L[j, j], then x_i -= L[j, i] x_j for i < j. */
+void orc_blocked_ltsolve(int n, const size_t *Lp, const int *Li, const double *Lx,
+                         const size_t *Li_ptr, const int *sup2col, int supNo,
+                         double *x, int nrhs);
 
 #ifdef __cplusplus
 }

@@ -21,6 +21,7 @@
 #include "sympiler/parsy/triangularSolve/Triangular_CSC.h"
 #include "sympiler/parsy/common/TreeUtils.h"
 #include "sympiler/parsy/symbolic/InspectionLevel_06.h"
+#include "sympiler/parsy/triangularSolve/Triangular_BCSC.h"
 
 namespace sym_lib {
 namespace parsy {
@@ -172,5 +173,34 @@ int ref_coarse_levelset6(int n, const int *eTree, int innerParts,
   delete[] finalNodePtr;
   delete[] parLevelSet;
   return finaLevelNo;
+}
+
+/* Supernodal (blocked CSC) forward solves, built with the reference's own
+ * dense kernels (SYM_BLAS).  Their multi-right-hand-side forms call an
+ * external BLAS, which is not built here: those calls land in
+ * ref_blas_missing and abort. */
+int ref_blocked_lsolve(int n, size_t *Lp, int *Li, double *Lx, size_t *Li_ptr,
+                       int *col2sup, int *sup2col, int supNo, double *x) {
+  return parsy::blockedLsolve(n, Lp, Li, Lx, 0, Li_ptr, col2sup, sup2col, supNo, x);
+}
+int ref_leveled_blocked_lsolve(int n, size_t *Lp, int *Li, double *Lx,
+                               size_t *Li_ptr, int *col2sup, int *sup2col,
+                               int supNo, double *x, int levels, int *levelPtr,
+                               int *levelSet) {
+  return parsy::leveledBlockedLsolve(n, Lp, Li, Lx, 0, Li_ptr, col2sup, sup2col,
+                                     supNo, x, levels, levelPtr, levelSet, 1);
+}
+int ref_h2_leveled_blocked_lsolve(int n, size_t *Lp, int *Li, double *Lx,
+                                  size_t *Li_ptr, int *col2sup, int *sup2col,
+                                  int supNo, double *x, int levels,
+                                  int *levelPtr, int *levelSet, int parts,
+                                  int *parPtr, int *partition) {
+  return parsy::H2LeveledBlockedLsolve(n, Lp, Li, Lx, 0, Li_ptr, col2sup, sup2col,
+                                       supNo, x, levels, levelPtr, levelSet,
+                                       parts, parPtr, partition, 1);
+}
+void ref_blas_missing(...) {
+  std::fprintf(stderr, "reference build: external BLAS routine called (not built)\n");
+  std::abort();
 }
 }

@@ -76,6 +76,19 @@ SIGNATURES = {
     "gbsym_coarse_levelset_tree": (_int, [_int, _vp, _vp, _int, _int, _int, _vp, _vp, _vp, _vp, _vp]),
     "gbsym_build_lbc": (_int, [_int, _vp, _vp, _vp, _int, _int, _int, _vp, _vp, _vp, _vp, _vp]),
     "gbsym_etree_lower_csr": (_int, [_int, _vp, _vp, _vp]),
+    "gbsym_parsy_blockedLsolve": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp]),
+    "gbsym_parsy_blockedLTsolve": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp]),
+    "gbsym_parsy_blockedLsolve_mrhs": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _int]),
+    "gbsym_parsy_blockedLTsolve_mrhs": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _int]),
+    "gbsym_parsy_leveledBlockedLsolve": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _vp, _vp, _int]),
+    "gbsym_parsy_H2LeveledBlockedLsolve": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _vp, _vp, _int, _vp, _vp, _int]),
+    "gbsym_parsy_H2LeveledBlockedLTsolve": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _vp, _vp, _int, _vp, _vp, _int]),
+    "gbsym_parsy_H2LeveledBlockedLsolve_mrhs": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _int, _vp, _vp, _int, _vp, _vp, _int, _int]),
+    "gbsym_parsy_H2LeveledBlockedLTsolve_mrhs": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _int, _vp, _vp, _int, _vp, _vp, _int, _int]),
+    "gbsym_sn_create": (_int, [_vp, _int, _vp, _vp, _vp, _vp, _vp, _int, _vp]),
+    "gbsym_sn_destroy": (_int, [_vp]),
+    "gbsym_sn_levels": (_int, [_vp, _vp, _vp]),
+    "gbsym_sn_solve": (_int, [_vp, _vp, _int, _int, _vp]),
     "gbsym_csr_create": (_int, [C.POINTER(_vp), _int, _int, _vp, _vp, _vp, _int, _int, _vp]),
     "gbsym_csr_destroy": (_int, [_vp]),
     "gbsym_csr_spmv": (_int, [_vp, _vp, _vp, _int, _vp]),

@@ -288,3 +288,91 @@ def block_diagonal(systems):
         cx[eoff[q]:eoff[q + 1]] = sx
     p[N] = E
     return N, p, ci, cx, off
+
+
+# ---- supernodal (blocked CSC) factors ------------------------------------
+
+@dataclass
+class Supernodal:
+    """A lower triangle in the blocked CSC layout of the reference's
+    supernodal solves (parsy::blockedLsolve and relatives): supernode s owns
+    columns sup2col[s] .. sup2col[s+1]-1 and the rows Li[Li_ptr[c0] ..
+    Li_ptr[c1]) (its own columns first); its values are a column-major
+    block of nSupR rows starting at Lx[Lp[c0]]."""
+    n: int
+    nsup: int
+    Lp: np.ndarray       # uint64[n+1]  (size_t)
+    Li: np.ndarray       # int32
+    Lx: np.ndarray       # float64
+    Li_ptr: np.ndarray   # uint64[n+1]  (size_t)
+    col2sup: np.ndarray  # int32[n]
+    sup2col: np.ndarray  # int32[nsup+1]
+
+    def dense(self) -> np.ndarray:
+        """The lower triangle as a dense array (unused storage ignored)."""
+        L = np.zeros((self.n, self.n))
+        for s in range(self.nsup):
+            c0, c1 = int(self.sup2col[s]), int(self.sup2col[s + 1])
+            r0, r1 = int(self.Li_ptr[c0]), int(self.Li_ptr[c1])
+            rows = self.Li[r0:r1]
+            nr = r1 - r0
+            blk = self.Lx[int(self.Lp[c0]):int(self.Lp[c0]) + nr * (c1 - c0)].reshape(c1 - c0, nr)
+            for j in range(c1 - c0):
+                for k in range(j, nr):
+                    L[rows[k], c0 + j] = blk[j, k]
+        return L
+
+
+def random_supernodal(nsup: int, max_width: int = 16, max_off: int = 40,
+                      rng: np.random.Generator | None = None, tree: bool = True) -> Supernodal:
+    """Seeded random supernodal lower triangle.  With ``tree`` the off-block
+    rows of a supernode lie in the columns of its ancestors in a random
+    supernode tree (the structure a Cholesky factor has); otherwise in any
+    later columns.  Diagonal blocks dominate so solutions stay bounded; the
+    unused upper halves of the diagonal blocks hold NaN, so a solve that
+    read them would show it."""
+    rng = np.random.default_rng(0) if rng is None else rng
+    widths = rng.integers(1, max_width + 1, nsup)
+    sup2col = np.concatenate([[0], np.cumsum(widths)]).astype(np.int32)
+    n = int(sup2col[-1])
+    parent = np.full(nsup, -1)
+    for s in range(nsup - 1):
+        parent[s] = int(rng.integers(s + 1, min(nsup, s + 1 + max(1, nsup // 8)) + 1)) if tree else -1
+        if parent[s] >= nsup:
+            parent[s] = -1
+    Lp = np.zeros(n + 1, dtype=np.uint64)
+    Li_ptr = np.zeros(n + 1, dtype=np.uint64)
+    col2sup = np.zeros(n, dtype=np.int32)
+    Li_parts, Lx_parts = [], []
+    rbase = vbase = 0
+    for s in range(nsup):
+        c0, c1 = int(sup2col[s]), int(sup2col[s + 1])
+        w = c1 - c0
+        if tree:
+            cand, a = [], parent[s]
+            while a >= 0:
+                cand.extend(range(int(sup2col[a]), int(sup2col[a + 1])))
+                a = parent[a]
+            cand = np.asarray(cand, dtype=np.int64)
+        else:
+            cand = np.arange(c1, n)
+        m = min(len(cand), int(rng.integers(0, max_off + 1)))
+        off = np.sort(rng.choice(cand, m, replace=False)) if m else np.zeros(0, dtype=np.int64)
+        rows = np.concatenate([np.arange(c0, c1), off]).astype(np.int32)
+        nr = len(rows)
+        blk = rng.uniform(-1.0, 1.0, (w, nr)) / (2.0 * (w + m + 1))
+        for j in range(w):
+            blk[j, :j] = np.nan
+            blk[j, j] = 1.0 + rng.uniform(0.0, 1.0)
+        col2sup[c0:c1] = s
+        Li_ptr[c0:c1] = rbase
+        for j in range(w):
+            Lp[c0 + j] = vbase + j * nr
+        Li_parts.append(rows)
+        Lx_parts.append(blk.reshape(-1))
+        rbase += nr
+        vbase += nr * w
+    Li_ptr[n] = rbase
+    Lp[n] = vbase
+    return Supernodal(n, nsup, Lp, np.concatenate(Li_parts), np.concatenate(Lx_parts), Li_ptr,
+                      col2sup, sup2col)

@@ -187,6 +187,45 @@ def host_solve_in_place(ptr: int) -> bool:
     return bool(lib().gbsym_host_solve_in_place(C.c_void_p(ptr)))
 
 
+
+class SupernodalPlan:
+    """A supernodal (blocked CSC) factor resident on the GPU: forward and
+    transposed solves on column-major device right-hand sides."""
+
+    def __init__(self, S, stream=None):
+        h = C.c_void_p()
+        arrs = [np.ascontiguousarray(S.Lp, np.uint64), np.ascontiguousarray(S.Li, np.int32),
+                np.ascontiguousarray(S.Lx, np.float64), np.ascontiguousarray(S.Li_ptr, np.uint64),
+                np.ascontiguousarray(S.sup2col, np.int32)]
+        check(lib().gbsym_sn_create(C.byref(h), int(S.n), *[a.ctypes.data_as(C.c_void_p) for a in arrs],
+                                    int(S.nsup), _stream(stream)), "gbsym_sn_create")
+        self._h = h
+        self.n = int(S.n)
+
+    def levels(self):
+        f, b = C.c_int(0), C.c_int(0)
+        check(lib().gbsym_sn_levels(self._h, C.byref(f), C.byref(b)), "gbsym_sn_levels")
+        return f.value, b.value
+
+    def solve(self, X, transposed=False, stream=None):
+        """In place on a CUDA float64 tensor of shape (n,) or (k, n) (k
+        right-hand sides, each contiguous: column-major n x k)."""
+        k = 1 if X.dim() == 1 else X.shape[0]
+        check(lib().gbsym_sn_solve(self._h, _dev_ptr(X, None, "X"), int(k), int(bool(transposed)),
+                                   _stream(stream)), "gbsym_sn_solve")
+        return X
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().gbsym_sn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
 class CsrPlan:
     """A CSR matrix resident on the GPU for SpMV."""
 

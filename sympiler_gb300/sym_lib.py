@@ -191,6 +191,63 @@ class parsy:  # noqa: N801 -- mirrors the reference's nested namespace
                          (_arr(eTree, _I32, "eTree"), _arr(nodeCost, _F64, "nodeCost")),
                          innerParts, minLevelDist, divRate, "getCoarseLevelSet_6")
 
+    # ---- supernodal (blocked CSC) solves: S is a matgen.Supernodal, x a
+    # float64 array of n (or n_rhs rows of n: column-major n x n_rhs) ----
+    @staticmethod
+    def _sn(S):
+        return (int(S.n), _p(_arr(S.Lp, np.uint64, "Lp")), _p(_arr(S.Li, _I32, "Li")),
+                _p(_arr(S.Lx, _F64, "Lx")), 0, _p(_arr(S.Li_ptr, np.uint64, "Li_ptr")),
+                _p(_arr(S.col2sup, _I32, "col2sup")), _p(_arr(S.sup2col, _I32, "sup2col")), int(S.nsup))
+
+    @staticmethod
+    def blockedLsolve(S, x):  # noqa: N802
+        """Triangular_BCSC.cpp:23-58 -- supernodal forward solve in place."""
+        x = _arr(x, _F64, "x", True)
+        return lib().gbsym_parsy_blockedLsolve(*parsy._sn(S), _p(x))
+
+    @staticmethod
+    def blockedLTsolve(S, x):  # noqa: N802
+        """Triangular_BCSC.cpp:124-184 -- supernodal transposed solve in place."""
+        x = _arr(x, _F64, "x", True)
+        return lib().gbsym_parsy_blockedLTsolve(*parsy._sn(S), _p(x))
+
+    @staticmethod
+    def blockedLsolve_mrhs(S, X, n_rhs, max_col=-1):  # noqa: N802
+        X = _arr(X, _F64, "X", True)
+        return lib().gbsym_parsy_blockedLsolve_mrhs(*parsy._sn(S), _p(X), int(n_rhs), int(max_col))
+
+    @staticmethod
+    def blockedLTsolve_mrhs(S, X, m_rhs, max_col=-1):  # noqa: N802
+        X = _arr(X, _F64, "X", True)
+        return lib().gbsym_parsy_blockedLTsolve_mrhs(*parsy._sn(S), _p(X), int(m_rhs), int(max_col))
+
+    @staticmethod
+    def leveledBlockedLsolve(S, x, levels, levelPtr, levelSet, chunk=1):  # noqa: N802,N803
+        x = _arr(x, _F64, "x", True)
+        lp, ls = _arr(levelPtr, _I32, "levelPtr"), _arr(levelSet, _I32, "levelSet")
+        return lib().gbsym_parsy_leveledBlockedLsolve(*parsy._sn(S), _p(x), int(levels), _p(lp), _p(ls),
+                                                      int(chunk))
+
+    @staticmethod
+    def H2LeveledBlockedLsolve(S, x, levels, levelPtr, parts, parPtr, partition, chunk=1,  # noqa: N802,N803
+                               transposed=False):
+        x = _arr(x, _F64, "x", True)
+        lp, pp, pa = (_arr(levelPtr, _I32, "levelPtr"), _arr(parPtr, _I32, "parPtr"),
+                      _arr(partition, _I32, "partition"))
+        fn = lib().gbsym_parsy_H2LeveledBlockedLTsolve if transposed else lib().gbsym_parsy_H2LeveledBlockedLsolve
+        return fn(*parsy._sn(S), _p(x), int(levels), _p(lp), None, int(parts), _p(pp), _p(pa), int(chunk))
+
+    @staticmethod
+    def H2LeveledBlockedLsolve_mrhs(S, X, n_rhs, levels, levelPtr, parts, parPtr, partition,  # noqa: N802,N803
+                                    chunk=1, max_col=-1, transposed=False):
+        X = _arr(X, _F64, "X", True)
+        lp, pp, pa = (_arr(levelPtr, _I32, "levelPtr"), _arr(parPtr, _I32, "parPtr"),
+                      _arr(partition, _I32, "partition"))
+        fn = (lib().gbsym_parsy_H2LeveledBlockedLTsolve_mrhs if transposed
+              else lib().gbsym_parsy_H2LeveledBlockedLsolve_mrhs)
+        return fn(*parsy._sn(S), _p(X), int(n_rhs), int(levels), _p(lp), None, int(parts), _p(pp), _p(pa),
+                  int(chunk), int(max_col))
+
     @staticmethod
     def lus_cr(n, nz_num, ia, ja, l, ua, r, z):
         """sparse_blas/parsy/gmres/mgmres.cpp:598-689 -- z = (LU)^{-1} r."""

@@ -71,6 +71,9 @@ int main(int argc, char **argv) {
     sym_lib::spic0_csr(n, v, p, i);
     sym_lib::parsy::lsolve(n, p, i, v, x);
     sym_lib::parsy::lus_cr(n, 1, p, i, v, i, x, y);
+    size_t zp[2] = {0, 1};
+    sym_lib::parsy::blockedLsolve(n, zp, i, v, 1, zp, i, p, 1, x);
+    sym_lib::parsy::H2LeveledBlockedLTsolve(n, zp, i, v, 1, zp, i, p, 1, x, 1, p, i, 1, p, i, 1);
     sym_lib::build_levelSet_CSC(1, p, i, lp, ls);
     delete[] lp; delete[] ls;
   }
