@@ -264,10 +264,13 @@ int gbsym_parsy_H2LeveledBlockedLTsolve_mrhs(
     int *levelPtr, int *levelSet, int parts, int *parPtr, int *partition,
     int chunk, int max_col);
 
-/* Supernodal plan: the factor resident on the GPU with its supernode level
- * schedules (host arrays in).  gbsym_sn_solve works on device memory, x
+/* Supernodal plan: the factor resident on the GPU with its solve task
+ * lists (host arrays in).  gbsym_sn_solve works on device memory, x
  * column-major n x k, forward (transposed = 0) or L^T (transposed = 1);
- * stream-ordered.  A supernode may be at most 5120 columns wide. */
+ * stream-ordered, one solve at a time per plan.  gbsym_sn_check
+ * synchronises the stream and returns (and clears) the plan's sticky
+ * device error: GBSYM_ERR_TIMEOUT if a bounded wait of an earlier solve
+ * gave up. */
 typedef struct gbsym_sn_s *gbsym_sn;
 int gbsym_sn_create(gbsym_sn *out, int n, const size_t *Lp, const int *Li,
                     const double *Lx, const size_t *Li_ptr, const int *sup2col,
@@ -275,6 +278,7 @@ int gbsym_sn_create(gbsym_sn *out, int n, const size_t *Lp, const int *Li,
 int gbsym_sn_destroy(gbsym_sn t);
 int gbsym_sn_levels(gbsym_sn t, int *forward_levels, int *transposed_levels);
 int gbsym_sn_solve(gbsym_sn t, double *x, int k, int transposed, void *stream);
+int gbsym_sn_check(gbsym_sn t, void *stream);
 
 /* ======================================================================== */
 /* Plans (device-resident).                                                 */

@@ -650,6 +650,35 @@ static double blk_row_dot(int ld, int ncol, const double *M, int k, const double
   return acc;
 }
 
+/* The off-block part of column q in the transposed solve: sum over the
+ * nb off-block rows (storage order) of col[r] * x[rows[r]], grouped as
+ * blk_row_dot groups a row: runs of 8, then 4, then 1; each run summed left
+ * to right, then added to a running value that starts at +0.  This order is
+ * this library's own: the reference's SYM_BLAS build has no transposed
+ * kernel of its own (blockedLTsolve, Triangular_BCSC.cpp:124-177, applies
+ * the forward kernels there and marks it FIXME). */
+static double blk_col_dot(int nb, const double *col, const int *rows, const double *x) {
+  double acc = 0.0;
+  int fc = 0;
+  while (fc < nb - 7) {
+    double s = x[rows[fc]] * col[fc];
+    for (int b = 1; b < 8; ++b) s = s + x[rows[fc + b]] * col[fc + b];
+    acc = acc + s;
+    fc += 8;
+  }
+  while (fc < nb - 3) {
+    double s = x[rows[fc]] * col[fc];
+    for (int b = 1; b < 4; ++b) s = s + x[rows[fc + b]] * col[fc + b];
+    acc = acc + s;
+    fc += 4;
+  }
+  while (fc < nb) {
+    acc = acc + x[rows[fc]] * col[fc];
+    fc += 1;
+  }
+  return acc;
+}
+
 /* Triangular_BCSC.cpp:23-58: per supernode in increasing order, the dense
  * diagonal solve, then the off-block product subtracted from the rows it
  * reaches. */
@@ -681,11 +710,8 @@ void orc_blocked_ltsolve(int n, const size_t *Lp, const int *Li, const double *L
       const int c0 = sup2col[s], c1 = sup2col[s + 1], w = c1 - c0;
       const int nr = (int)(Li_ptr[c1] - Li_ptr[c0]);
       const double *M = Lx + Lp[c0];
-      for (int q = 0; q < w; ++q) {
-        double v = xj[c0 + q];
-        for (int k = w; k < nr; ++k) v = v - M[(size_t)q * nr + k] * xj[Li[Li_ptr[c0] + k]];
-        xj[c0 + q] = v;
-      }
+      for (int q = 0; q < w; ++q)
+        xj[c0 + q] = xj[c0 + q] - blk_col_dot(nr - w, M + (size_t)q * nr + w, Li + Li_ptr[c0] + w, xj);
       for (int q = w - 1; q >= 0; --q) {
         const double v = xj[c0 + q] / M[(size_t)q * nr + q];
         xj[c0 + q] = v;

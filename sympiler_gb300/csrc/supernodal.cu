@@ -7,187 +7,383 @@
 // columns first, and its values a column-major block of nr = Li_ptr[c1] -
 // Li_ptr[c0] rows at Lx + Lp[c0].  x is column-major n x k.
 //
-// Forward solve.  The reference (blockedLsolve, :23-58) walks supernodes in
+// Forward order.  The reference (blockedLsolve, :23-58) walks supernodes in
 // order: a dense solve of the diagonal block (dlsolve_blas_nonUnit), then
-// the off-block rows' products (dmatvec_blas) pushed into the rows they
-// reach.  Every row therefore receives its subtractions in increasing
-// source order.  Here a supernode pulls them instead: for each of its rows,
-// the contributions of its sources in increasing order, each product
-// formed in dmatvec_blas's grouping -- so the results are the reference's,
-// bit for bit, while supernodes of one level run in parallel without
-// atomics (the reference's leveled variants subtract under `omp atomic`,
-// whose order varies).  The dense diagonal solve follows
-// dlsolve_blas_nonUnit's grouping (runs of 8, 4, 2, 1 columns; left-to-right
-// subtraction chains; IEEE division).  Both kernels' groupings are restated
-// from parsy/triangularSolve/BLAS.cpp:12-185.
+// the off-block rows' products (dmatvec_blas) subtracted from the rows they
+// reach.  Row q of a supernode therefore sees: the products of its sources
+// in increasing source order, then -- dlsolve_blas_nonUnit's runs of 8, 4,
+// 2, 1 columns unrolled -- one rounded product and one rounded difference
+// per earlier column of its own block, in column order, and finally an
+// IEEE division.  Each off-block product is dmatvec_blas's grouping: column
+// runs of 8 while 8 remain, then 4, then single columns, each run summed
+// left to right, the run sums added to a running +0.  Both groupings are
+// restated from parsy/triangularSolve/BLAS.cpp:12-185; results here are the
+// reference's, bit for bit.
 //
-// Transposed solve.  The reference's SYM_BLAS build applies the forward
-// kernels here (its own FIXME); its BLAS build calls dgemv/dtrsm, whose
-// summation order is the library's.  This file solves L^T x = b in an order
-// of its own: per supernode column j, x_j minus the off-block rows'
-// products in storage order, then the diagonal block's transpose backward.
+// Transposed order (this library's own: under SYM_BLAS the reference's
+// blockedLTsolve, Triangular_BCSC.cpp:124-177, applies the forward kernels
+// and is marked FIXME).  Supernodes in decreasing order; column q: x_q minus
+// its off-block column's product with the solved rows, in the same run
+// grouping; then one rounded product and difference per later column of the
+// diagonal block, from the last; then the division.
 //
-// Supernodes are scheduled by the levels of the supernode dependency DAG
-// (one launch per level; a block per supernode).
+// Execution.  FP64 on this part issues one warp instruction per 67.5 cycles
+// per SM sub-partition, so a supernode of w columns is far too much work for
+// one block: the top separator of a 3D grid alone holds w^2/2 products on a
+// critical path of w dependent (multiply, subtract, divide) steps.  One
+// persistent launch works through a task list in which every task is one
+// warp's:
+//   forward  D(s, i)  rows 32i..32i+31 of s's diagonal block: pull the
+//                     sources' products (in source order), apply the columns
+//                     of tiles 0..i-1 as they are published, solve the
+//                     tile, publish it;
+//            P(s, o)  32/H off-block rows of s, H lanes per row splitting
+//                     its column runs; the run sums are chained in order
+//                     through shuffles.  Products go to a contribution
+//                     buffer, one slot per (source, off-block row).
+//   transposed O(s, a)  32/H columns' off-block products, x_q updated in
+//                     place;  T(s, i)  tiles from the last, mirror of D.
+// Tasks are listed by supernode level, each supernode's tasks together, and
+// taken in list order through one atomic counter; a task waits only on
+// earlier tasks (bounded waits on per-supernode counters), so the warps
+// that hold the tasks it waits on are running and no wait can deadlock.
+// Counters grow across solves (a solve's targets are multiples of its
+// epoch), so nothing is cleared between solves.
 #include <algorithm>
+#include <climits>
 #include <memory>
 #include <vector>
 
 #include "common.cuh"
+#include "exec_common.cuh"
+
+namespace gbsym {
+struct SnTask {
+  int kind;  // low byte: kind; bits 8.. : target count (forward products)
+  int sup, a, b;
+};
+}  // namespace gbsym
 
 struct gbsym_sn_s {
   int n = 0, nsup = 0, nlev = 0, nblev = 0, max_w = 0;
+  int nftask = 0, ntt = 0;  // tasks per right-hand-side group, forward / transposed
+  int grid1 = 0, grid8 = 0;  // blocks of the persistent launch, per instantiation
+  int groups = 0;            // right-hand-side groups the counters are laid out for
+  unsigned long long ef = 0, et = 0;  // solves since the counters were cleared
+  unsigned long long fctr = 0, tctr = 0;  // task-counter values those solves left
+  long long ncontrib = 0;
+  size_t contrib_k = 0;
   std::vector<int> h_lev_ptr, h_blev_ptr;
-  gbsym::DBuf<int> c0, nr, rb;          // per supernode: first column, rows, row base
-  gbsym::DBuf<long long> vb;            // per supernode: value base (Lp[c0])
-  gbsym::DBuf<int> rows;                // Li
-  gbsym::DBuf<double> vals;             // Lx
-  gbsym::DBuf<int> pull_ptr, pull_src, pull_k;  // forward: per column, (source, row position)
-  gbsym::DBuf<int> lev_set, blev_set;   // supernodes in forward / backward level order
+  gbsym::DBuf<int> c0, nr, hf, need_in, n_ot, tg_ptr, tg;
+  gbsym::DBuf<long long> rb, vb, coff;
+  gbsym::DBuf<int> rows;
+  gbsym::DBuf<double> vals;
+  gbsym::DBuf<int> pull_ptr, pull_idx;
+  gbsym::DBuf<gbsym::SnTask> ftask, ttask;
+  gbsym::DBuf<int> ftb, ttb, gt_tg;
+  gbsym::DBuf<unsigned long long> flags;  // [fwd ctr, tr ctr] + 4 x nsup x groups
+  gbsym::DBuf<double> contrib;
+  gbsym::DBuf<int> err;
 };
 
 namespace gbsym {
 namespace {
 
-constexpr int kSnBlock = 128;
-constexpr int kSnSmem = 5120;  // values of shared memory per block (40 KB)
+constexpr int kSnWarps = 4;
+constexpr unsigned kFull = 0xffffffffu;
+constexpr long long kSnWaitCycles = 1ll << 32;  // about two seconds
+enum { kD = 0, kP = 1, kO = 2, kT = 3 };
 
-__device__ __forceinline__ double dm(double a, double b) { return __dmul_rn(a, b); }
-__device__ __forceinline__ double da(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ double ds(double a, double b) { return __dsub_rn(a, b); }
+struct SnView {
+  int n, k, groups, ntask, nblk;
+  const int *c0, *nr, *hsplit, *need_in, *n_ot, *tg_ptr, *tg;
+  const long long *rb, *vb, *coff;
+  const int *rows;
+  const double *vals;
+  const int *pull_ptr, *pull_idx;
+  const SnTask *task;
+  const int *tb, *gt_tg;
+  unsigned long long *ctr, *done, *in;
+  double *x, *contrib;
+  long long ncontrib;
+  unsigned long long epoch, base;
+  int *err;
+};
 
-// One off-block row's product with the source's solved values, in
-// dmatvec_blas's grouping: runs of 8 columns while 8 remain past the
-// current one, then runs of 4, then single columns; each run summed left to
-// right, then added to the running value, which starts at +0.
-__device__ double row_dot(const double *__restrict__ M, int ld, int ncol, int k, const double *__restrict__ v) {
-  double acc = 0.0;
-  int fc = 0;
-  while (fc < ncol - 7) {
-    double s = dm(v[fc], M[(size_t)fc * ld + k]);
-#pragma unroll
-    for (int b = 1; b < 8; ++b) s = da(s, dm(v[fc + b], M[(size_t)(fc + b) * ld + k]));
-    acc = da(acc, s);
-    fc += 8;
-  }
-  while (fc < ncol - 3) {
-    double s = dm(v[fc], M[(size_t)fc * ld + k]);
-#pragma unroll
-    for (int b = 1; b < 4; ++b) s = da(s, dm(v[fc + b], M[(size_t)(fc + b) * ld + k]));
-    acc = da(acc, s);
-    fc += 4;
-  }
-  while (fc < ncol) {
-    acc = da(acc, dm(v[fc], M[(size_t)fc * ld + k]));
-    ++fc;
-  }
-  return acc;
+// Exact arithmetic as fused multiply-adds (bit-identical to the separate
+// operations, signed zeros included): RN(a*b) = fma(a, b, -0) and
+// RN(s + p) = fma(p, 1, s).  Inline PTX is never executed speculatively,
+// so guarded lanes and right-hand sides cost no FP64 issue.
+__device__ __forceinline__ double xmul(double a, double b) {
+  double r;
+  asm("fma.rn.f64 %0, %1, %2, 0d8000000000000000;" : "=d"(r) : "d"(a), "d"(b));
+  return r;
+}
+__device__ __forceinline__ double xadd(double s, double p) {
+  double r;
+  asm("fma.rn.f64 %0, %1, 0d3FF0000000000000, %2;" : "=d"(r) : "d"(p), "d"(s));
+  return r;
+}
+__device__ __forceinline__ double xsub(double s, double p) {
+  double r;
+  asm("fma.rn.f64 %0, %1, 0dBFF0000000000000, %2;" : "=d"(r) : "d"(p), "d"(s));
+  return r;
+}
+// RN(s + RN(a*b))
+__device__ __forceinline__ double xmadd(double s, double a, double b) { return xadd(s, xmul(a, b)); }
+
+__device__ __forceinline__ unsigned long long ld_acq64(const unsigned long long *p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_rel64(unsigned long long *p) {
+  asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(p) : "memory");
 }
 
-// Forward: one block per supernode of the level.  Right-hand sides are done
-// kc columns at a time so that the w x kc values fit in shared memory.
-__global__ void __launch_bounds__(kSnBlock)
-k_sn_forward(const int *__restrict__ lev_set, int base, const int *__restrict__ c0s, const int *__restrict__ nrs,
-             const long long *__restrict__ vbs, const double *__restrict__ Lx, const int *__restrict__ pull_ptr,
-             const int *__restrict__ pull_src, const int *__restrict__ pull_k, double *__restrict__ x, int n,
-             int k) {
-  __shared__ double rhs[kSnSmem];
-  __shared__ double xg[8 * 64];
-  const int t = lev_set[base + blockIdx.x];
-  const int c0 = c0s[t], w = c0s[t + 1] - c0, ld = nrs[t];
-  const double *M = Lx + vbs[t];
-  const int kc = max(1, min(min(k, 64), kSnSmem / w));
-  for (int j0 = 0; j0 < k; j0 += kc) {
-    const int kk = min(kc, k - j0);
-    // pull: each row's subtractions from its sources in increasing order
-    for (int idx = threadIdx.x; idx < w * kk; idx += blockDim.x) {
-      const int q = idx % w, jj = idx / w;
-      const int r = c0 + q;
-      double *xc = x + (size_t)(j0 + jj) * n;
-      double acc = xc[r];
-      for (int p = pull_ptr[r]; p < pull_ptr[r + 1]; ++p) {
-        const int s = pull_src[p];
-        const int sc0 = c0s[s];
-        acc = ds(acc, row_dot(Lx + vbs[s], nrs[s], c0s[s + 1] - sc0, pull_k[p], xc + sc0));
-      }
-      rhs[jj * w + q] = acc;
+// Every lane waits (with its own acquire) until *f >= want.  Gives up after
+// about two seconds, recording GBSYM_ERR_TIMEOUT, or at once when another
+// wait has; the task then runs on, so every counter still reaches its
+// target and the launch ends.
+__device__ bool sn_wait(const unsigned long long *f, unsigned long long want, int *err) {
+  if (__all_sync(kFull, ld_acq64(f) >= want)) return true;
+  const long long t0 = __shfl_sync(kFull, clock64(), 0);
+  for (;;) {
+    __nanosleep(40);
+    if (__all_sync(kFull, ld_acq64(f) >= want)) return true;
+    if (__any_sync(kFull, ld_relaxed(err) != 0)) return false;
+    if (__shfl_sync(kFull, clock64() - t0 > kSnWaitCycles, 0)) {
+      if ((threadIdx.x & 31) == 0) atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
+      return false;
     }
-    __syncthreads();
-    // the diagonal block, in runs of 8, 4, 2, 1 columns
-    int fc = 0;
-    while (fc < w) {
-      const int g = fc < w - 7 ? 8 : fc < w - 3 ? 4 : fc < w - 1 ? 2 : 1;
-      for (int jj = threadIdx.x; jj < kk; jj += blockDim.x) {
-        double *rv = rhs + jj * w;
-        for (int a = 0; a < g; ++a) {
-          double v = rv[fc + a];
-          for (int b = 0; b < a; ++b) v = ds(v, dm(xg[jj * 8 + b], M[(size_t)(fc + b) * ld + fc + a]));
-          v = __ddiv_rn(v, M[(size_t)(fc + a) * ld + fc + a]);
-          xg[jj * 8 + a] = v;
-          rv[fc + a] = v;
+  }
+}
+
+// After the warp's stores: make them visible before the task is counted.
+__device__ __forceinline__ void sn_fence() {
+  __threadfence();
+  __syncwarp();
+}
+
+// Column (or row) runs of dmatvec_blas: w / 8 runs of 8, then at most one
+// of 4, then single ones.
+struct Runs {
+  int n8, n4, nruns;
+  __device__ explicit Runs(int w) {
+    n8 = w >> 3;
+    const int rem = w & 7;
+    n4 = rem >= 4;
+    nruns = n8 + n4 + (rem - 4 * n4);
+  }
+  __device__ void at(int r, int &start, int &size) const {
+    if (r < n8) {
+      start = r << 3;
+      size = 8;
+    } else if (n4 && r == n8) {
+      start = n8 << 3;
+      size = 4;
+    } else {
+      start = (n8 << 3) + 4 * n4 + (r - n8 - n4);
+      size = 1;
+    }
+  }
+};
+
+// The grouped product sum of one row (forward: entries E[c*estride] and
+// values xb[c]) or one column (transposed: entries E[r] and values
+// xb[idx[r]]), for kr right-hand sides xstride apart.  Lane (rho, h)
+// computes the run sums of runs h, h + H, ...; the running value, which
+// starts at +0, adds them in run order, taken from the H lanes of its row
+// by shuffles.
+template <int KR, bool TR>
+__device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool act, const double *__restrict__ E,
+                                            size_t estride, const int *__restrict__ idx, const double *xb,
+                                            size_t xstride, int kr, double (&acc)[KR]) {
+  const Runs R(len);
+#pragma unroll
+  for (int j = 0; j < KR; ++j) acc[j] = 0.0;
+  for (int base = 0; base < R.nruns; base += H) {
+    const int r = base + h;
+    double s[KR];
+#pragma unroll
+    for (int j = 0; j < KR; ++j) s[j] = 0.0;
+    if (act && r < R.nruns) {
+      int cs, sz;
+      R.at(r, cs, sz);
+      {
+        const double m = __ldg(E + (size_t)cs * estride);
+        const size_t xo = TR ? (size_t)idx[cs] : (size_t)cs;
+#pragma unroll
+        for (int j = 0; j < KR; ++j)
+          if (j < kr) s[j] = xmul(__ldcg(xb + (size_t)j * xstride + xo), m);
+      }
+      for (int b = 1; b < sz; ++b) {
+        const int c = cs + b;
+        const double m = __ldg(E + (size_t)c * estride);
+        const size_t xo = TR ? (size_t)idx[c] : (size_t)c;
+#pragma unroll
+        for (int j = 0; j < KR; ++j)
+          if (j < kr) s[j] = xmadd(s[j], __ldcg(xb + (size_t)j * xstride + xo), m);
+      }
+    }
+    const int top = min(H, R.nruns - base);
+    for (int hh = 0; hh < top; ++hh) {
+#pragma unroll
+      for (int j = 0; j < KR; ++j)
+        if (j < kr) {
+          const double sv = __shfl_sync(kFull, s[j], rho * H + hh);
+          if (act) acc[j] = xadd(acc[j], sv);
+        }
+    }
+  }
+}
+
+template <int KR>
+__global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
+  const int lane = threadIdx.x & 31;
+  const unsigned long long total = (unsigned long long)V.ntask * V.groups;
+  for (;;) {
+    unsigned long long u = 0;
+    if (lane == 0) u = atomicAdd(V.ctr, 1ull) - V.base;
+    u = __shfl_sync(kFull, u, 0);
+    if (u >= total) break;
+    // supernode block b holds groups x (tb[b+1] - tb[b]) task slots
+    int lo = 0, hi = V.nblk;
+    while (hi - lo > 1) {
+      const int mid = (lo + hi) >> 1;
+      if ((unsigned long long)V.tb[mid] * V.groups <= u) lo = mid;
+      else hi = mid;
+    }
+    const int nb = V.tb[lo + 1] - V.tb[lo];
+    const unsigned long long off = u - (unsigned long long)V.tb[lo] * V.groups;
+    const int g = (int)(off / nb);
+    const SnTask T = V.task[V.tb[lo] + (int)(off % nb)];
+    const int kind = T.kind & 0xff, t = T.sup;
+    const int j0 = g * KR, kr = min(KR, V.k - j0);
+    const int c0 = V.c0[t], w = V.c0[t + 1] - c0, ld = V.nr[t];
+    const int nt = (w + 31) >> 5;
+    const double *__restrict__ M = V.vals + V.vb[t];
+    double *const xg = V.x + (size_t)j0 * V.n;
+    const size_t fi = (size_t)t * V.groups + g;
+    const unsigned long long e1 = V.epoch - 1;
+
+    if (kind == kD || kind == kT) {
+      const bool fwd = kind == kD;
+      const int i = T.a;
+      const int q = (i << 5) + lane;
+      const bool act = q < w;
+      sn_wait(V.in + fi, V.epoch * (unsigned long long)(fwd ? V.need_in[t] : V.n_ot[t]), V.err);
+      double v[KR];
+#pragma unroll
+      for (int j = 0; j < KR; ++j) v[j] = (act && j < kr) ? __ldcg(xg + (size_t)j * V.n + c0 + q) : 0.0;
+      if (fwd && act) {
+        // the sources' products, in increasing source order
+        for (int p = V.pull_ptr[c0 + q]; p < V.pull_ptr[c0 + q + 1]; ++p) {
+          const size_t ci = (size_t)V.pull_idx[p];
+#pragma unroll
+          for (int j = 0; j < KR; ++j)
+            if (j < kr) v[j] = xsub(v[j], __ldcg(V.contrib + (size_t)(j0 + j) * V.ncontrib + ci));
         }
       }
-      __syncthreads();
-      const int rem = w - fc - g;
-      for (int idx = threadIdx.x; idx < rem * kk; idx += blockDim.x) {
-        const int q = fc + g + idx % rem, jj = idx / rem;
-        double v = rhs[jj * w + q];
-        for (int b = 0; b < g; ++b) v = ds(v, dm(xg[jj * 8 + b], M[(size_t)(fc + b) * ld + q]));
-        rhs[jj * w + q] = v;
+      // earlier tiles as they are published (forward: 0..i-1; transposed:
+      // nt-1 down to i+1), then this tile
+      const int steps = fwd ? i : nt - 1 - i;
+      for (int step = 0; step <= steps; ++step) {
+        const int J = fwd ? step : nt - 1 - step;
+        const bool own = step == steps;
+        const int cnt = min(32, w - (J << 5));
+        double xl[KR];
+#pragma unroll
+        for (int j = 0; j < KR; ++j) xl[j] = 0.0;
+        if (!own) {
+          sn_wait(V.done + fi, e1 * nt + step + 1, V.err);
+#pragma unroll
+          for (int j = 0; j < KR; ++j)
+            if (j < kr && lane < cnt) xl[j] = __ldcg(xg + (size_t)j * V.n + c0 + (J << 5) + lane);
+        }
+        double d = 1.0, y = 1.0;
+        if (own && act) {
+          d = __ldg(M + (size_t)q * ld + q);
+          y = __drcp_rn(d);
+        }
+        for (int cc = 0; cc < cnt; ++cc) {
+          const int c = fwd ? cc : cnt - 1 - cc;
+          const int col = (J << 5) + c;
+          // forward: entry (row q, column col); transposed: (row col, column q)
+          const bool upd = act && (!own || (fwd ? lane > c : lane < c));
+          const double m = upd ? __ldg(fwd ? M + (size_t)col * ld + q : M + (size_t)q * ld + col) : 0.0;
+#pragma unroll
+          for (int j = 0; j < KR; ++j)
+            if (j < kr) {
+              if (own && lane == c) v[j] = div_by(v[j], d, y);
+              const double xc = __shfl_sync(kFull, own ? v[j] : xl[j], c);
+              if (upd) v[j] = xsub(v[j], xmul(m, xc));
+            }
+        }
       }
-      __syncthreads();
-      fc += g;
+      if (act) {
+#pragma unroll
+        for (int j = 0; j < KR; ++j)
+          if (j < kr) xg[(size_t)j * V.n + c0 + q] = v[j];
+      }
+      sn_fence();
+      if (lane == 0) red_rel64(V.done + fi);
+    } else {
+      const int H = V.hsplit[t];
+      const int rho = lane / H, h = lane % H;
+      double acc[KR];
+      if (kind == kP) {
+        // off-block rows w + a + rho: products with the supernode's solution
+        sn_wait(V.done + fi, V.epoch * nt, V.err);
+        const int o = T.a + rho;
+        const bool act = o < ld - w;
+        grouped_sum<KR, false>(w, H, rho, h, act, M + w + o, ld, nullptr, xg + c0, V.n, kr, acc);
+        if (act && h == 0) {
+#pragma unroll
+          for (int j = 0; j < KR; ++j)
+            if (j < kr) V.contrib[(size_t)(j0 + j) * V.ncontrib + V.coff[t] + o] = acc[j];
+        }
+        sn_fence();
+        if (lane == 0) {
+          const int cnt = T.kind >> 8;
+          for (int e = 0; e < cnt; ++e) red_rel64(V.in + (size_t)V.gt_tg[T.b + e] * V.groups + g);
+        }
+      } else {
+        // columns a + rho: off-block products with the solved rows below
+        for (int e = V.tg_ptr[t]; e < V.tg_ptr[t + 1]; ++e) {
+          const int s = V.tg[e];
+          const int nts = (V.c0[s + 1] - V.c0[s] + 31) >> 5;
+          sn_wait(V.done + (size_t)s * V.groups + g, V.epoch * nts, V.err);
+        }
+        const int col = T.a + rho;
+        const bool act = col < w;
+        grouped_sum<KR, true>(ld - w, H, rho, h, act, M + (size_t)col * ld + w, 1, V.rows + V.rb[t] + w, xg, V.n,
+                              kr, acc);
+        if (act && h == 0) {
+#pragma unroll
+          for (int j = 0; j < KR; ++j)
+            if (j < kr) {
+              double *xp = xg + (size_t)j * V.n + c0 + col;
+              *xp = xsub(__ldcg(xp), acc[j]);
+            }
+        }
+        sn_fence();
+        if (lane == 0) red_rel64(V.in + fi);
+      }
     }
-    for (int idx = threadIdx.x; idx < w * kk; idx += blockDim.x) {
-      const int q = idx % w, jj = idx / w;
-      x[(size_t)(j0 + jj) * n + c0 + q] = rhs[jj * w + q];
-    }
-    __syncthreads();
   }
 }
 
-// Transposed: per supernode column j, x_j minus the off-block rows'
-// products in storage order; then the diagonal block's transpose backward.
-__global__ void __launch_bounds__(kSnBlock)
-k_sn_transposed(const int *__restrict__ lev_set, int base, const int *__restrict__ c0s, const int *__restrict__ nrs,
-                const int *__restrict__ rbs, const long long *__restrict__ vbs, const int *__restrict__ rows,
-                const double *__restrict__ Lx, double *__restrict__ x, int n, int k) {
-  __shared__ double rhs[kSnSmem];
-  const int t = lev_set[base + blockIdx.x];
-  const int c0 = c0s[t], w = c0s[t + 1] - c0, ld = nrs[t];
-  const int *rw = rows + rbs[t];
-  const double *M = Lx + vbs[t];
-  const int kc = max(1, min(k, kSnSmem / w));
-  for (int j0 = 0; j0 < k; j0 += kc) {
-    const int kk = min(kc, k - j0);
-    for (int idx = threadIdx.x; idx < w * kk; idx += blockDim.x) {
-      const int q = idx % w, jj = idx / w;
-      const double *xc = x + (size_t)(j0 + jj) * n;
-      double acc = xc[c0 + q];
-      for (int r = w; r < ld; ++r) acc = ds(acc, dm(M[(size_t)q * ld + r], xc[rw[r]]));
-      rhs[jj * w + q] = acc;
-    }
-    __syncthreads();
-    for (int q = w - 1; q >= 0; --q) {
-      for (int jj = threadIdx.x; jj < kk; jj += blockDim.x)
-        rhs[jj * w + q] = __ddiv_rn(rhs[jj * w + q], M[(size_t)q * ld + q]);
-      __syncthreads();
-      for (int idx = threadIdx.x; idx < q * kk; idx += blockDim.x) {
-        const int i = idx % q, jj = idx / q;
-        rhs[jj * w + i] = ds(rhs[jj * w + i], dm(M[(size_t)i * ld + q], rhs[jj * w + q]));
-      }
-      __syncthreads();
-    }
-    for (int idx = threadIdx.x; idx < w * kk; idx += blockDim.x) {
-      const int q = idx % w, jj = idx / w;
-      x[(size_t)(j0 + jj) * n + c0 + q] = rhs[jj * w + q];
-    }
-    __syncthreads();
-  }
+// Lanes per row for a product over len entries: enough that no lane sums
+// more than 64 runs, at most 32.
+int split_for(int len) {
+  const int rem = len & 7, n4 = rem >= 4;
+  const int nruns = len / 8 + n4 + (rem - 4 * n4);
+  int H = 1;
+  while (H < 32 && (nruns + H - 1) / H > 64) H *= 2;
+  return H;
 }
 
-// Levels of a DAG over supernodes given as successor lists in increasing
-// node order (forward) or predecessor lists in decreasing order (backward).
 void levels_from(const std::vector<int> &lev, int nsup, std::vector<int> &ptr, std::vector<int> &set) {
   int nl = 0;
   for (int v : lev) nl = std::max(nl, v + 1);
@@ -197,6 +393,13 @@ void levels_from(const std::vector<int> &lev, int nsup, std::vector<int> &ptr, s
   set.assign(nsup, 0);
   std::vector<int> fill(ptr.begin(), ptr.end() - 1);
   for (int s = 0; s < nsup; ++s) set[fill[lev[s]]++] = s;
+}
+
+template <int KR>
+int sn_grid() {
+  int per_sm = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sn<KR>, kSnWarps * 32, 0));
+  return std::max(1, per_sm) * num_sms();
 }
 
 gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, const size_t *Li_ptr,
@@ -209,10 +412,10 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
   t->nsup = nsup;
   if (n == 0) return t.release();
   GB_CHECK(sup2col[0] == 0 && sup2col[nsup] == n, GBSYM_ERR_BAD_MATRIX);
-  std::vector<int> c0(nsup + 1), nr(nsup), rb(nsup);
-  std::vector<long long> vb(nsup);
-  std::vector<int> col2sup(n);
+  std::vector<int> c0(nsup + 1), nr(nsup), col2sup(n);
+  std::vector<long long> rb(nsup), vb(nsup), coff(nsup);
   size_t nvals = 0;
+  long long ncontrib = 0;
   for (int q = 0; q < nsup; ++q) {
     const int a = sup2col[q], z = sup2col[q + 1];
     GB_CHECK(z > a, GBSYM_ERR_BAD_MATRIX);
@@ -220,8 +423,10 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
     GB_CHECK(r1 >= r0 + (size_t)(z - a) && r1 - r0 < (size_t)1 << 30, GBSYM_ERR_BAD_MATRIX);
     c0[q] = a;
     nr[q] = (int)(r1 - r0);
-    rb[q] = (int)r0;
+    rb[q] = (long long)r0;
     vb[q] = (long long)Lp[a];
+    coff[q] = ncontrib;
+    ncontrib += nr[q] - (z - a);
     for (int j = 0; j < z - a; ++j) {
       GB_CHECK(Li[r0 + j] == a + j, GBSYM_ERR_BAD_MATRIX);  // the diagonal block's rows first
       col2sup[a + j] = q;
@@ -232,9 +437,10 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
     t->max_w = std::max(t->max_w, z - a);
   }
   c0[nsup] = n;
-  GB_CHECK(t->max_w <= kSnSmem, GBSYM_ERR_UNSUPPORTED);
+  GB_CHECK(ncontrib < INT_MAX, GBSYM_ERR_UNSUPPORTED);
+  t->ncontrib = ncontrib;
   const size_t nrows = Li_ptr[n];
-  // forward pull lists (sources ascending) and both level schedules
+  // pull lists (sources ascending) and both level schedules
   std::vector<int> cnt(n + 1, 0), flev(nsup, 0), blev(nsup, 0);
   for (int q = 0; q < nsup; ++q) {
     const int w = c0[q + 1] - c0[q];
@@ -249,17 +455,12 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
     for (int k = w; k < nr[q]; ++k) blev[q] = std::max(blev[q], blev[col2sup[Li[rb[q] + k]]] + 1);
   }
   for (int r = 0; r < n; ++r) cnt[r + 1] += cnt[r];
-  std::vector<int> psrc(std::max(cnt[n], 1)), pk(std::max(cnt[n], 1));
+  std::vector<int> pidx(std::max(cnt[n], 1));
   {
     std::vector<int> fill(cnt.begin(), cnt.end() - 1);
     for (int q = 0; q < nsup; ++q) {
       const int w = c0[q + 1] - c0[q];
-      for (int k = w; k < nr[q]; ++k) {
-        const int r = Li[rb[q] + k];
-        psrc[fill[r]] = q;
-        pk[fill[r]] = k;
-        fill[r]++;
-      }
+      for (int k = w; k < nr[q]; ++k) pidx[fill[Li[rb[q] + k]]++] = (int)(coff[q] + (k - w));
     }
   }
   std::vector<int> lset, bset;
@@ -267,40 +468,159 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
   levels_from(blev, nsup, t->h_blev_ptr, bset);
   t->nlev = (int)t->h_lev_ptr.size() - 1;
   t->nblev = (int)t->h_blev_ptr.size() - 1;
+  // task lists, by supernode level.  Lanes per row (forward products) and
+  // per column (transposed) live in one array, the transposed half second.
+  std::vector<int> hs(2 * nsup), need_in(nsup, 0), n_ot(nsup, 0), tg_ptr(nsup + 1, 0), tg, gt_tg;
+  std::vector<SnTask> ft, tt;
+  std::vector<int> ftb(nsup + 1), ttb(nsup + 1);
+  for (int q = 0; q < nsup; ++q) {
+    const int w = c0[q + 1] - c0[q];
+    hs[q] = split_for(w);
+    hs[nsup + q] = split_for(nr[q] - w);
+    int prev = -1;
+    for (int k = w; k < nr[q]; ++k) {
+      const int u = col2sup[Li[rb[q] + k]];
+      if (u != prev) tg.push_back(u);
+      prev = u;
+    }
+    tg_ptr[q + 1] = (int)tg.size();
+  }
+  for (int b = 0; b < nsup; ++b) {
+    const int q = lset[b], w = c0[q + 1] - c0[q], nb = nr[q] - w, nt = (w + 31) / 32;
+    ftb[b] = (int)ft.size();
+    for (int i = 0; i < nt; ++i) ft.push_back({kD, q, i, 0});
+    const int R = 32 / hs[q];
+    for (int o = 0; o < nb; o += R) {
+      const int start = (int)gt_tg.size();
+      int prev = -1;
+      for (int k = o; k < std::min(nb, o + R); ++k) {
+        const int u = col2sup[Li[rb[q] + w + k]];
+        if (u != prev) {
+          gt_tg.push_back(u);
+          need_in[u]++;
+        }
+        prev = u;
+      }
+      ft.push_back({kP | (((int)gt_tg.size() - start) << 8), q, o, start});
+    }
+  }
+  ftb[nsup] = (int)ft.size();
+  for (int b = 0; b < nsup; ++b) {
+    const int q = bset[b], w = c0[q + 1] - c0[q], nb = nr[q] - w, nt = (w + 31) / 32;
+    ttb[b] = (int)tt.size();
+    if (nb > 0) {
+      const int R = 32 / hs[nsup + q];
+      for (int a = 0; a < w; a += R, ++n_ot[q]) tt.push_back({kO, q, a, 0});
+    }
+    for (int i = nt - 1; i >= 0; --i) tt.push_back({kT, q, i, 0});
+  }
+  ttb[nsup] = (int)tt.size();
+  t->nftask = (int)ft.size();
+  t->ntt = (int)tt.size();
   upload(t->c0, c0.data(), c0.size(), false, s);
   upload(t->nr, nr.data(), nr.size(), false, s);
   upload(t->rb, rb.data(), rb.size(), false, s);
   upload(t->vb, vb.data(), vb.size(), false, s);
+  upload(t->coff, coff.data(), coff.size(), false, s);
   upload(t->rows, Li, nrows, false, s);
   upload(t->vals, Lx, nvals, false, s);
   upload(t->pull_ptr, cnt.data(), cnt.size(), false, s);
-  upload(t->pull_src, psrc.data(), psrc.size(), false, s);
-  upload(t->pull_k, pk.data(), pk.size(), false, s);
-  upload(t->lev_set, lset.data(), lset.size(), false, s);
-  upload(t->blev_set, bset.data(), bset.size(), false, s);
+  upload(t->pull_idx, pidx.data(), pidx.size(), false, s);
+  upload(t->hf, hs.data(), hs.size(), false, s);
+  upload(t->need_in, need_in.data(), need_in.size(), false, s);
+  upload(t->n_ot, n_ot.data(), n_ot.size(), false, s);
+  upload(t->tg_ptr, tg_ptr.data(), tg_ptr.size(), false, s);
+  if (tg.empty()) tg.push_back(0);
+  upload(t->tg, tg.data(), tg.size(), false, s);
+  if (gt_tg.empty()) gt_tg.push_back(0);
+  upload(t->gt_tg, gt_tg.data(), gt_tg.size(), false, s);
+  upload(t->ftask, ft.data(), ft.size(), false, s);
+  upload(t->ttask, tt.data(), tt.size(), false, s);
+  upload(t->ftb, ftb.data(), ftb.size(), false, s);
+  upload(t->ttb, ttb.data(), ttb.size(), false, s);
+  t->err.alloc(2);
+  GB_CUDA(cudaMemsetAsync(t->err.p, 0, 2 * sizeof(int), s));
+  t->grid1 = sn_grid<1>();
+  t->grid8 = sn_grid<8>();
   GB_CUDA(cudaStreamSynchronize(s));
   return t.release();
 }
 
 void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) {
   if (t->n == 0 || k == 0) return;
-  if (!transposed) {
-    for (int l = 0; l < t->nlev; ++l) {
-      const int a = t->h_lev_ptr[l], z = t->h_lev_ptr[l + 1];
-      k_sn_forward<<<z - a, kSnBlock, 0, s>>>(t->lev_set.p, a, t->c0.p, t->nr.p, t->vb.p, t->vals.p,
-                                              t->pull_ptr.p, t->pull_src.p, t->pull_k.p, x, t->n, k);
-      check_launch();
-    }
-  } else {
-    // backward level 0 holds the supernodes whose rows below are all final
-    // (none below them): they go first
-    for (int l = 0; l < t->nblev; ++l) {
-      const int a = t->h_blev_ptr[l], z = t->h_blev_ptr[l + 1];
-      k_sn_transposed<<<z - a, kSnBlock, 0, s>>>(t->blev_set.p, a, t->c0.p, t->nr.p, t->rb.p, t->vb.p,
-                                                 t->rows.p, t->vals.p, x, t->n, k);
-      check_launch();
-    }
+  const int KR = k == 1 ? 1 : 8;
+  const int G = (k + KR - 1) / KR;
+  const size_t per = (size_t)t->nsup * G;
+  if (G != t->groups) {
+    t->flags.alloc(2 + 4 * per);
+    GB_CUDA(cudaMemsetAsync(t->flags.p, 0, t->flags.n * sizeof(unsigned long long), s));
+    t->groups = G;
+    t->ef = t->et = t->fctr = t->tctr = 0;
   }
+  if (!transposed && t->ncontrib > 0 && t->contrib_k < (size_t)k) {
+    t->contrib.alloc((size_t)t->ncontrib * k);
+    t->contrib_k = k;
+  }
+  const int grid = KR == 1 ? t->grid1 : t->grid8;
+  const unsigned long long nwarps = (unsigned long long)grid * kSnWarps;
+  SnView V{};
+  V.n = t->n;
+  V.k = k;
+  V.groups = G;
+  V.nblk = t->nsup;
+  V.c0 = t->c0.p;
+  V.nr = t->nr.p;
+  V.hsplit = t->hf.p + (transposed ? t->nsup : 0);
+  V.need_in = t->need_in.p;
+  V.n_ot = t->n_ot.p;
+  V.tg_ptr = t->tg_ptr.p;
+  V.tg = t->tg.p;
+  V.rb = t->rb.p;
+  V.vb = t->vb.p;
+  V.coff = t->coff.p;
+  V.rows = t->rows.p;
+  V.vals = t->vals.p;
+  V.pull_ptr = t->pull_ptr.p;
+  V.pull_idx = t->pull_idx.p;
+  V.gt_tg = t->gt_tg.p;
+  V.x = x;
+  V.contrib = t->contrib.p;
+  V.ncontrib = t->ncontrib;
+  V.err = t->err.p;
+  unsigned long long *f = t->flags.p;
+  if (!transposed) {
+    V.ntask = t->nftask;
+    V.task = t->ftask.p;
+    V.tb = t->ftb.p;
+    V.ctr = f;
+    V.done = f + 2;
+    V.in = f + 2 + per;
+    V.base = t->fctr;
+    t->fctr += (unsigned long long)t->nftask * G + nwarps;  // every warp takes one slot past the end
+    V.epoch = ++t->ef;
+  } else {
+    V.ntask = t->ntt;
+    V.task = t->ttask.p;
+    V.tb = t->ttb.p;
+    V.ctr = f + 1;
+    V.done = f + 2 + 2 * per;
+    V.in = f + 2 + 3 * per;
+    V.base = t->tctr;
+    t->tctr += (unsigned long long)t->ntt * G + nwarps;
+    V.epoch = ++t->et;
+  }
+  if (KR == 1) k_sn<1><<<grid, kSnWarps * 32, 0, s>>>(V);
+  else k_sn<8><<<grid, kSnWarps * 32, 0, s>>>(V);
+  check_launch();
+}
+
+int sn_read_error(gbsym_sn_s *t, cudaStream_t s) {
+  if (!t->err.p) return 0;
+  int h[2] = {0, 0};
+  GB_CUDA(cudaMemcpyAsync(h, t->err.p, sizeof(h), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  if (h[0]) GB_CUDA(cudaMemsetAsync(t->err.p, 0, 2 * sizeof(int), s));
+  return h[0];
 }
 
 // Every supernode once; each dependency finished in an earlier coarse
@@ -348,6 +668,8 @@ void sn_dropin(int n, const size_t *Lp, const int *Li, const double *Lx, const s
   DBuf<double> dx;
   upload(dx, x, (size_t)n * k, false, s);
   sn_solve(t.get(), dx.p, k, transposed, s);
+  const int code = sn_read_error(t.get(), s);
+  if (code) throw Err{code};
   GB_CUDA(cudaMemcpyAsync(x, dx.p, (size_t)n * k * sizeof(double), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
 }
@@ -396,6 +718,13 @@ int gbsym_sn_solve(gbsym_sn t, double *x, int k, int transposed, void *stream) {
   if (!t || (!x && t->n && k)) return GBSYM_ERR_NULL_ARG;
   if (k < 0) return GBSYM_ERR_SIZE;
   return guarded([&] { sn_solve(t, x, k, transposed != 0, (cudaStream_t)stream); });
+}
+
+int gbsym_sn_check(gbsym_sn t, void *stream) {
+  if (!t) return GBSYM_ERR_NULL_ARG;
+  int code = 0;
+  const int st = guarded([&] { code = sn_read_error(t, (cudaStream_t)stream); });
+  return st != GBSYM_OK ? st : code;
 }
 
 #define GBSYM_SN_ARGS                                                                                      \

@@ -376,3 +376,100 @@ def random_supernodal(nsup: int, max_width: int = 16, max_off: int = 40,
     Lp[n] = vbase
     return Supernodal(n, nsup, Lp, np.concatenate(Li_parts), np.concatenate(Lx_parts), Li_ptr,
                       col2sup, sup2col)
+
+
+def nd_supernodal(nx: int, ny: int, nz: int = 1, leaf: int = 64,
+                  rng: np.random.Generator | None = None) -> Supernodal:
+    """Seeded supernodal lower triangle with the structure of the Cholesky
+    factor of the 7-point (5-point when nz = 1) Laplacian on an nx x ny x nz
+    grid in geometric nested-dissection order.
+
+    Boxes are bisected across their longest side until they hold at most
+    ``leaf`` nodes; each separator plane and each leaf box is one supernode,
+    numbered after both halves (post-order).  A supernode's off-block rows
+    are the grid neighbours of its box outside the box -- nodes of ancestor
+    separators -- which is exactly the union of its columns' structures in
+    the filled graph, so blocks are dense as a supernodal Cholesky stores
+    them.  Values are random: off-diagonals of row r uniform in
+    (-1, 1) / (entries of row r), diagonals in [2, 3), so solutions stay
+    bounded; the unused upper halves of the diagonal blocks hold NaN."""
+    rng = np.random.default_rng(0) if rng is None else rng
+    dims = (nx, ny, nz)
+    sups = []  # (own box, enclosing box), post-order
+
+    def rec(box):
+        size = [b - a for a, b in box]
+        if size[0] * size[1] * size[2] <= leaf:
+            sups.append((box, box))
+            return
+        d = int(np.argmax(size))
+        m = (box[d][0] + box[d][1]) // 2
+        lo, hi, sep = list(box), list(box), list(box)
+        lo[d], hi[d], sep[d] = (box[d][0], m), (m + 1, box[d][1]), (m, m + 1)
+        for half in (lo, hi):
+            if half[d][1] > half[d][0]:
+                rec(tuple(half))
+        sups.append((tuple(sep), box))
+
+    rec(((0, nx), (0, ny), (0, nz)))
+    n = nx * ny * nz
+    new = np.empty(n, dtype=np.int64)  # grid node (x + nx*(y + ny*z)) -> column
+
+    def nodes(box):
+        (x0, x1), (y0, y1), (z0, z1) = box
+        z, y, x = np.meshgrid(np.arange(z0, z1), np.arange(y0, y1), np.arange(x0, x1), indexing="ij")
+        return (x + nx * (y + ny * z)).reshape(-1)
+
+    sup2col = np.zeros(len(sups) + 1, dtype=np.int32)
+    c = 0
+    for s, (own, _) in enumerate(sups):
+        g = nodes(own)
+        new[g] = np.arange(c, c + len(g))
+        c += len(g)
+        sup2col[s + 1] = c
+    rows_of = []
+    for own, box in sups:
+        faces = []
+        for d in range(3):
+            for side, at in ((0, box[d][0] - 1), (1, box[d][1])):
+                if 0 <= at < dims[d]:
+                    f = list(box)
+                    f[d] = (at, at + 1)
+                    faces.append(new[nodes(tuple(f))])
+        c0 = int(new[nodes(own)].min())
+        w = int(np.prod([b - a for a, b in own]))
+        off = np.sort(np.concatenate(faces)) if faces else np.zeros(0, dtype=np.int64)
+        rows_of.append(np.concatenate([np.arange(c0, c0 + w), off]).astype(np.int32))
+    nsup = len(sups)
+    # entries per row, for the off-diagonal scale
+    cnt = np.zeros(n, dtype=np.float64)
+    for s in range(nsup):
+        w = int(sup2col[s + 1] - sup2col[s])
+        r = rows_of[s]
+        cnt[r[w:]] += w
+        cnt[r[:w]] += np.arange(w)
+    cnt = np.maximum(cnt, 1.0)
+    Lp = np.zeros(n + 1, dtype=np.uint64)
+    Li_ptr = np.zeros(n + 1, dtype=np.uint64)
+    col2sup = np.zeros(n, dtype=np.int32)
+    Lx_parts = []
+    rbase = vbase = 0
+    for s in range(nsup):
+        c0, c1 = int(sup2col[s]), int(sup2col[s + 1])
+        w = c1 - c0
+        r = rows_of[s]
+        nr = len(r)
+        blk = rng.uniform(-1.0, 1.0, (w, nr)) / cnt[r][None, :]
+        jc, kr = np.tril_indices(w, -1)
+        blk[jc, kr] = np.nan  # column j's rows k < j: the unused upper half
+        blk[np.arange(w), np.arange(w)] = 2.0 + rng.uniform(0.0, 1.0, w)
+        col2sup[c0:c1] = s
+        Li_ptr[c0:c1] = rbase
+        Lp[c0:c1] = vbase + np.arange(w, dtype=np.uint64) * np.uint64(nr)
+        Lx_parts.append(blk.reshape(-1))
+        rbase += nr
+        vbase += nr * w
+    Li_ptr[n] = rbase
+    Lp[n] = vbase
+    return Supernodal(n, nsup, Lp, np.concatenate(rows_of), np.concatenate(Lx_parts), Li_ptr,
+                      col2sup, sup2col)

@@ -215,6 +215,11 @@ class SupernodalPlan:
                                    _stream(stream)), "gbsym_sn_solve")
         return X
 
+    def check(self, stream=None):
+        """Synchronise and raise if a bounded device wait of an earlier
+        solve gave up."""
+        check(lib().gbsym_sn_check(self._h, _stream(stream)), "gbsym_sn_check")
+
     def close(self):
         if getattr(self, "_h", None):
             lib().gbsym_sn_destroy(self._h)

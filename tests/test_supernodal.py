@@ -73,7 +73,61 @@ def test_restatement_against_dense_solves(orc):
         assert np.allclose(x, np.linalg.solve(D.T, b), rtol=1e-12, atol=1e-12)
 
 
+def test_nested_dissection_factors_match_reference_and_dense(orc, ref):
+    for t, (dims, leaf) in enumerate([((12, 10, 9), 16), ((20, 1, 1), 4), ((9, 9, 1), 8), ((7, 6, 5), 27)]):
+        S = mg.nd_supernodal(*dims, leaf=leaf, rng=np.random.default_rng(t))
+        D = S.dense()
+        b = np.random.default_rng(50 + t).standard_normal(S.n)
+        x1 = b.copy()
+        orc.blocked_lsolve(S, x1)
+        x2 = b.copy()
+        assert ref.blocked_lsolve(S, x2) == 1
+        assert np.array_equal(x1, x2), dims
+        assert np.abs(D @ x1 - b).max() <= 1e-13
+        x3 = b.copy()
+        orc.blocked_ltsolve(S, x3)
+        assert np.abs(D.T @ x3 - b).max() <= 1e-13
+
+
 # ---- GPU --------------------------------------------------------------------
+
+@pytest.mark.gpu
+def test_gpu_nested_dissection_factor_repeated_solves(gpu, orc):
+    """A 24^3 grid's factor (separators up to 576 columns, off-block rows
+    split across lanes): forward and transposed, one and many right-hand
+    sides, several solves on one plan -- the task counters carry over
+    between solves."""
+    import torch
+    from sympiler_gb300.plans import SupernodalPlan
+    S = mg.nd_supernodal(24, 24, 24, leaf=64, rng=np.random.default_rng(3))
+    assert np.diff(S.sup2col).max() == 576
+    P = SupernodalPlan(S)
+    rng = np.random.default_rng(4)
+    for rep, (k, transposed) in enumerate([(1, False), (1, True), (8, False), (1, False), (13, True),
+                                           (13, False), (1, True), (8, True)]):
+        X = rng.standard_normal((k, S.n))
+        W = X.copy()
+        (orc.blocked_ltsolve if transposed else orc.blocked_lsolve)(S, W if k > 1 else W[0])
+        Xd = torch.from_numpy(X.copy()).cuda()
+        P.solve(Xd if k > 1 else Xd[0], transposed=transposed)
+        P.check()
+        assert np.array_equal(Xd.cpu().numpy(), W), (rep, k, transposed)
+
+
+@pytest.mark.gpu
+def test_gpu_nested_dissection_2d_wide_separator(gpu, orc):
+    from sympiler_gb300 import sym_lib
+    S = mg.nd_supernodal(150, 130, 1, leaf=16, rng=np.random.default_rng(6))
+    assert np.diff(S.sup2col).max() == 130
+    b = np.random.default_rng(7).standard_normal(S.n)
+    for fn, ofn in ((sym_lib.parsy.blockedLsolve, orc.blocked_lsolve),
+                    (sym_lib.parsy.blockedLTsolve, orc.blocked_ltsolve)):
+        want = b.copy()
+        ofn(S, want)
+        x = b.copy()
+        assert fn(S, x) == 1
+        assert np.array_equal(x, want)
+
 
 @pytest.mark.gpu
 def test_gpu_blocked_solves_bit_exact(gpu, orc):
@@ -163,7 +217,7 @@ def test_gpu_supernodal_plan_many_rhs_and_wide_supernodes(gpu, orc):
             (orc.blocked_ltsolve if transposed else orc.blocked_lsolve)(S, W if k > 1 else W[0])
             Xd = torch.from_numpy(X.copy()).cuda()
             P.solve(Xd if k > 1 else Xd[0], transposed=transposed)
-            torch.cuda.synchronize()
+            P.check()
             assert np.array_equal(Xd.cpu().numpy(), W), (k, transposed)
 
 
