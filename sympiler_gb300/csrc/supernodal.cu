@@ -82,11 +82,13 @@ struct gbsym_sn_s {
   gbsym::DBuf<gbsym::SnTask> ftask, ttask;
   gbsym::DBuf<int> ftb, ttb, gt_tg;
   gbsym::DBuf<unsigned long long> flags;  // [fwd ctr, tr ctr] + 4 x nsup x groups
-  gbsym::DBuf<double> contrib;
+  gbsym::DBuf<double> contrib, yscr;
   gbsym::DBuf<int> err;
 };
 
 namespace gbsym {
+void fill_sentinel(void *y, size_t bytes, cudaStream_t s);  // exec_syncfree.cu
+
 namespace {
 
 constexpr int kSnWarps = 4;
@@ -104,7 +106,7 @@ struct SnView {
   const SnTask *task;
   const int *tb, *gt_tg;
   unsigned long long *ctr, *done, *in;
-  double *x, *contrib;
+  double *x, *contrib, *y;
   long long ncontrib;
   unsigned long long epoch, base;
   int *err;
@@ -139,6 +141,52 @@ __device__ __forceinline__ unsigned long long ld_acq64(const unsigned long long 
 }
 __device__ __forceinline__ void red_rel64(unsigned long long *p) {
   asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(p) : "memory");
+}
+
+// The scratch copy of x that tiles of a supernode poll: all ones until
+// the value is stored (a NaN that no division produces).
+__device__ __forceinline__ bool unsolved(double v) { return __double_as_longlong(v) == -1ll; }
+__device__ __forceinline__ double ld_rlx_f64(const double *p) {
+  double v;
+  asm volatile("ld.relaxed.gpu.global.f64 %0, [%1];" : "=d"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_rlx_f64(double *p, double v) {
+  asm volatile("st.relaxed.gpu.global.f64 [%0], %1;" ::"l"(p), "d"(v) : "memory");
+}
+__device__ __forceinline__ void cp_async8(double *dst, const double *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// a / b correctly rounded, given y = RN(1/b): Markstein's three FMAs
+// (P. Markstein, IBM J. Res. Dev. 34(1), 1990).  The theorem needs every
+// intermediate normal: b's exponent in [3, 2043], a's in [63, 2043] and
+// within 1000 of b's.  The lane precomputes the window of a's exponent that
+// its b allows ([lo, hi]; empty as 4096, 4096 when b itself is out of
+// range), so the check is one unsigned compare beside the FMAs; outside it,
+// IEEE division, in a call (a branch the compiler cannot turn into
+// predicated FP64 work, which this part would issue on every lane).
+__device__ __noinline__ double ieee_div(double a, double b) { return __ddiv_rn(a, b); }
+struct DivWindow {
+  int lo, hi;
+  __device__ explicit DivWindow(double b) {
+    const int eb = (int)((__double_as_longlong(b) >> 52) & 0x7ff);
+    const bool valid = eb >= 3 && eb <= 2043;
+    lo = valid ? max(63, eb - 1000) : 4096;
+    hi = valid ? min(2043, eb + 1000) : 4096;
+  }
+};
+__device__ __forceinline__ double quotient(double a, double b, double y, const DivWindow &W) {
+  double q;
+  asm("fma.rn.f64 %0, %1, %2, 0d8000000000000000;" : "=d"(q) : "d"(a), "d"(y));
+  const double r = __fma_rn(-q, b, a);
+  double res = __fma_rn(r, y, q);
+  const int ea = (int)((__double_as_longlong(a) >> 52) & 0x7ff);
+  if ((unsigned)(ea - W.lo) > (unsigned)(W.hi - W.lo)) res = ieee_div(a, b);
+  return res;
 }
 
 // Every lane waits (with its own acquire) until *f >= want.  Gives up after
@@ -194,7 +242,7 @@ struct Runs {
 // xb[idx[r]]), for kr right-hand sides xstride apart.  Lane (rho, h)
 // computes the run sums of runs h, h + H, ...; the running value, which
 // starts at +0, adds them in run order, taken from the H lanes of its row
-// by shuffles.
+// by shuffles.  A run of 8 issues all its loads before its arithmetic.
 template <int KR, bool TR>
 __device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool act, const double *__restrict__ E,
                                             size_t estride, const int *__restrict__ idx, const double *xb,
@@ -207,7 +255,27 @@ __device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool
     double s[KR];
 #pragma unroll
     for (int j = 0; j < KR; ++j) s[j] = 0.0;
-    if (act && r < R.nruns) {
+    if (act && r < R.n8) {
+      const int cs = r << 3;
+      double m[8];
+      size_t xo[8];
+#pragma unroll
+      for (int b = 0; b < 8; ++b) {
+        m[b] = __ldg(E + (size_t)(cs + b) * estride);
+        xo[b] = TR ? (size_t)__ldg(idx + cs + b) : (size_t)(cs + b);
+      }
+#pragma unroll
+      for (int j = 0; j < KR; ++j)
+        if (j < kr) {
+          double xv[8];
+#pragma unroll
+          for (int b = 0; b < 8; ++b) xv[b] = __ldcg(xb + (size_t)j * xstride + xo[b]);
+          double a = xmul(xv[0], m[0]);
+#pragma unroll
+          for (int b = 1; b < 8; ++b) a = xmadd(a, xv[b], m[b]);
+          s[j] = a;
+        }
+    } else if (act && r < R.nruns) {
       int cs, sz;
       R.at(r, cs, sz);
       {
@@ -240,6 +308,7 @@ __device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool
 
 template <int KR>
 __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
+  __shared__ double sm_own[kSnWarps][32][32];
   const int lane = threadIdx.x & 31;
   const unsigned long long total = (unsigned long long)V.ntask * V.groups;
   for (;;) {
@@ -265,59 +334,131 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
     const double *__restrict__ M = V.vals + V.vb[t];
     double *const xg = V.x + (size_t)j0 * V.n;
     const size_t fi = (size_t)t * V.groups + g;
-    const unsigned long long e1 = V.epoch - 1;
 
     if (kind == kD || kind == kT) {
       const bool fwd = kind == kD;
       const int i = T.a;
       const int q = (i << 5) + lane;
       const bool act = q < w;
+      const int cnt_own = min(32, w - (i << 5));
+      double *const yg = V.y + (size_t)j0 * V.n;
+      // this tile's own entries, in the order the solve uses them, go to
+      // shared memory while the warp waits (forward: row q, columns 32i + c;
+      // transposed: column q, rows 32i + c from the last)
+      double(*so)[32] = sm_own[threadIdx.x >> 5];
+#pragma unroll
+      for (int cc = 0; cc < 32; ++cc) {
+        const int c = fwd ? cc : cnt_own - 1 - cc;
+        const bool upd = act && cc < cnt_own && (fwd ? lane > c : lane < c);
+        if (upd) cp_async8(&so[cc][lane], fwd ? M + (size_t)((i << 5) + c) * ld + q : M + (size_t)q * ld + (i << 5) + c);
+        else so[cc][lane] = 0.0;
+      }
+      cp_async_commit();
+      double d = 1.0, y = 1.0;
+      if (act) {
+        d = __ldg(M + (size_t)q * ld + q);
+        y = __drcp_rn(d);
+      }
       sn_wait(V.in + fi, V.epoch * (unsigned long long)(fwd ? V.need_in[t] : V.n_ot[t]), V.err);
       double v[KR];
 #pragma unroll
       for (int j = 0; j < KR; ++j) v[j] = (act && j < kr) ? __ldcg(xg + (size_t)j * V.n + c0 + q) : 0.0;
       if (fwd && act) {
-        // the sources' products, in increasing source order
-        for (int p = V.pull_ptr[c0 + q]; p < V.pull_ptr[c0 + q + 1]; ++p) {
-          const size_t ci = (size_t)V.pull_idx[p];
+        // the sources' products, in increasing source order, 8 loads at a time
+        const int p1 = V.pull_ptr[c0 + q + 1];
+        for (int p = V.pull_ptr[c0 + q]; p < p1; p += 8) {
+          size_t ci[8];
 #pragma unroll
-          for (int j = 0; j < KR; ++j)
-            if (j < kr) v[j] = xsub(v[j], __ldcg(V.contrib + (size_t)(j0 + j) * V.ncontrib + ci));
-        }
-      }
-      // earlier tiles as they are published (forward: 0..i-1; transposed:
-      // nt-1 down to i+1), then this tile
-      const int steps = fwd ? i : nt - 1 - i;
-      for (int step = 0; step <= steps; ++step) {
-        const int J = fwd ? step : nt - 1 - step;
-        const bool own = step == steps;
-        const int cnt = min(32, w - (J << 5));
-        double xl[KR];
-#pragma unroll
-        for (int j = 0; j < KR; ++j) xl[j] = 0.0;
-        if (!own) {
-          sn_wait(V.done + fi, e1 * nt + step + 1, V.err);
-#pragma unroll
-          for (int j = 0; j < KR; ++j)
-            if (j < kr && lane < cnt) xl[j] = __ldcg(xg + (size_t)j * V.n + c0 + (J << 5) + lane);
-        }
-        double d = 1.0, y = 1.0;
-        if (own && act) {
-          d = __ldg(M + (size_t)q * ld + q);
-          y = __drcp_rn(d);
-        }
-        for (int cc = 0; cc < cnt; ++cc) {
-          const int c = fwd ? cc : cnt - 1 - cc;
-          const int col = (J << 5) + c;
-          // forward: entry (row q, column col); transposed: (row col, column q)
-          const bool upd = act && (!own || (fwd ? lane > c : lane < c));
-          const double m = upd ? __ldg(fwd ? M + (size_t)col * ld + q : M + (size_t)q * ld + col) : 0.0;
+          for (int u = 0; u < 8; ++u) ci[u] = p + u < p1 ? (size_t)__ldg(V.pull_idx + p + u) : 0;
 #pragma unroll
           for (int j = 0; j < KR; ++j)
             if (j < kr) {
-              if (own && lane == c) v[j] = div_by(v[j], d, y);
-              const double xc = __shfl_sync(kFull, own ? v[j] : xl[j], c);
-              if (upd) v[j] = xsub(v[j], xmul(m, xc));
+              const double *cb = V.contrib + (size_t)(j0 + j) * V.ncontrib;
+              double cv[8];
+#pragma unroll
+              for (int u = 0; u < 8; ++u) cv[u] = p + u < p1 ? __ldcg(cb + ci[u]) : 0.0;
+#pragma unroll
+              for (int u = 0; u < 8; ++u)
+                if (p + u < p1) v[j] = xsub(v[j], cv[u]);
+            }
+        }
+      }
+      // earlier tiles (forward: 0..i-1; transposed: nt-1 down to i+1), each
+      // column applied as soon as its value appears in the scratch copy
+      const int steps = fwd ? i : nt - 1 - i;
+      bool failed = false;
+      for (int step = 0; step < steps; ++step) {
+        const int J = fwd ? step : nt - 1 - step;
+        const int cnt = min(32, w - (J << 5));
+        double m[32];
+#pragma unroll
+        for (int cc = 0; cc < 32; ++cc) {
+          const int c = fwd ? cc : cnt - 1 - cc;
+          m[cc] = (act && cc < cnt) ? __ldg(fwd ? M + (size_t)((J << 5) + c) * ld + q : M + (size_t)q * ld + (J << 5) + c)
+                                    : 0.0;
+        }
+        const unsigned inside = cnt == 32 ? kFull : (1u << cnt) - 1u;
+        int applied = 0;
+        long long t0 = 0;
+        while (applied < cnt) {
+          double xl[KR];
+          bool rdy = true;
+#pragma unroll
+          for (int j = 0; j < KR; ++j) {
+            xl[j] = 0.0;
+            if (j < kr && lane < cnt) {
+              xl[j] = ld_rlx_f64(yg + (size_t)j * V.n + c0 + (J << 5) + lane);
+              rdy = rdy && !unsolved(xl[j]);
+            }
+          }
+          // columns ready in the order they are applied
+          unsigned r = __ballot_sync(kFull, rdy) & inside;
+          if (!fwd) r = __brev(r) >> (32 - cnt);
+          const int pre = failed ? cnt : min(cnt, __ffs(~r) == 0 ? 32 : __ffs(~r) - 1);
+#pragma unroll
+          for (int cc = 0; cc < 32; ++cc) {
+            if (cc >= applied && cc < pre) {
+              const int c = fwd ? cc : cnt - 1 - cc;
+#pragma unroll
+              for (int j = 0; j < KR; ++j)
+                if (j < kr) {
+                  const double xc = __shfl_sync(kFull, xl[j], c);
+                  if (act) v[j] = xsub(v[j], xmul(m[cc], xc));
+                }
+            }
+          }
+          if (pre == applied) {
+            if (t0 == 0) t0 = __shfl_sync(kFull, clock64(), 0);
+            __nanosleep(20);
+            if (__any_sync(kFull, ld_relaxed(V.err) != 0)) failed = true;
+            if (__shfl_sync(kFull, clock64() - t0 > kSnWaitCycles, 0)) {
+              if (lane == 0) atomicCAS(V.err, 0, GBSYM_ERR_TIMEOUT);
+              failed = true;
+            }
+          }
+          applied = pre;
+        }
+      }
+      // this tile: lane c divides, the warp applies the quotient, and lane
+      // c publishes it at once for the tiles that wait on it
+      const DivWindow dw(d);
+      cp_async_wait_all();
+      __syncwarp();
+#pragma unroll
+      for (int cc = 0; cc < 32; ++cc) {
+        if (cc < cnt_own) {
+          const int c = fwd ? cc : cnt_own - 1 - cc;
+          const bool upd = act && (fwd ? lane > c : lane < c);
+          const double mc = so[cc][lane];
+#pragma unroll
+          for (int j = 0; j < KR; ++j)
+            if (j < kr) {
+              if (lane == c) v[j] = quotient(v[j], d, y, dw);
+              const double xc = __shfl_sync(kFull, v[j], c);
+              if (upd) v[j] = xsub(v[j], xmul(mc, xc));
+              // (a NaN with the sentinel's bits would read as unsolved)
+              if (lane == c)
+                st_rlx_f64(yg + (size_t)j * V.n + c0 + q, unsolved(xc) ? __longlong_as_double(0x7ff8000000000000ll) : xc);
             }
         }
       }
@@ -561,6 +702,8 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
     t->contrib.alloc((size_t)t->ncontrib * k);
     t->contrib_k = k;
   }
+  if (t->yscr.n < (size_t)t->n * k) t->yscr.alloc((size_t)t->n * k);
+  fill_sentinel(t->yscr.p, (size_t)t->n * k * sizeof(double), s);
   const int grid = KR == 1 ? t->grid1 : t->grid8;
   const unsigned long long nwarps = (unsigned long long)grid * kSnWarps;
   SnView V{};
@@ -585,6 +728,7 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
   V.gt_tg = t->gt_tg.p;
   V.x = x;
   V.contrib = t->contrib.p;
+  V.y = t->yscr.p;
   V.ncontrib = t->ncontrib;
   V.err = t->err.p;
   unsigned long long *f = t->flags.p;
