@@ -651,31 +651,35 @@ static double blk_row_dot(int ld, int ncol, const double *M, int k, const double
 }
 
 /* The off-block part of column q in the transposed solve: sum over the
- * nb off-block rows (storage order) of col[r] * x[rows[r]], grouped as
- * blk_row_dot groups a row: runs of 8, then 4, then 1; each run summed left
- * to right, then added to a running value that starts at +0.  This order is
- * this library's own: the reference's SYM_BLAS build has no transposed
- * kernel of its own (blockedLTsolve, Triangular_BCSC.cpp:124-177, applies
- * the forward kernels there and marks it FIXME). */
+ * nb off-block rows of col[r] * x[rows[r]], taken from the LAST row
+ * backward and grouped as blk_row_dot groups a row: runs of 8 while 8
+ * remain, then 4, then 1; each run summed in that order, then added to a
+ * running value that starts at +0.  This order is this library's own (its
+ * GPU solve consumes the ancestors' unknowns as they appear, top down): the
+ * reference's SYM_BLAS build has no transposed kernel of its own
+ * (blockedLTsolve, Triangular_BCSC.cpp:124-177, applies the forward
+ * kernels there and marks it FIXME). */
 static double blk_col_dot(int nb, const double *col, const int *rows, const double *x) {
   double acc = 0.0;
   int fc = 0;
+#define RP(e) (nb - 1 - (e))
   while (fc < nb - 7) {
-    double s = x[rows[fc]] * col[fc];
-    for (int b = 1; b < 8; ++b) s = s + x[rows[fc + b]] * col[fc + b];
+    double s = x[rows[RP(fc)]] * col[RP(fc)];
+    for (int b = 1; b < 8; ++b) s = s + x[rows[RP(fc + b)]] * col[RP(fc + b)];
     acc = acc + s;
     fc += 8;
   }
   while (fc < nb - 3) {
-    double s = x[rows[fc]] * col[fc];
-    for (int b = 1; b < 4; ++b) s = s + x[rows[fc + b]] * col[fc + b];
+    double s = x[rows[RP(fc)]] * col[RP(fc)];
+    for (int b = 1; b < 4; ++b) s = s + x[rows[RP(fc + b)]] * col[RP(fc + b)];
     acc = acc + s;
     fc += 4;
   }
   while (fc < nb) {
-    acc = acc + x[rows[fc]] * col[fc];
+    acc = acc + x[rows[RP(fc)]] * col[RP(fc)];
     fc += 1;
   }
+#undef RP
   return acc;
 }
 

@@ -126,7 +126,7 @@ void orc_blocked_lsolve(int n, const size_t *Lp, const int *Li, const double *Lx
                         double *x, int nrhs);
 /* Transposed (backward) solve L^T x = b on the same storage: supernodes in
  * decreasing order; per supernode column j, x_j minus the sum over the
- * off-block rows r (storage order) of L[r, j] x_r, grouped as dmatvec_blas
+ * off-block rows r (from the last) of L[r, j] x_r, grouped as dmatvec_blas
  * groups a row (runs of 8, 4, 1; run sums added to a running +0); then the diagonal block's transpose backward, column j from the
  * last: x_j /= L[j, j], then x_i -= L[j, i] x_j for i < j. */
 void orc_blocked_ltsolve(int n, const size_t *Lp, const int *Li, const double *Lx,

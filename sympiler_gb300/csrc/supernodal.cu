@@ -24,8 +24,9 @@
 // blockedLTsolve, Triangular_BCSC.cpp:124-177, applies the forward kernels
 // and is marked FIXME).  Supernodes in decreasing order; column q: x_q minus
 // its off-block column's product with the solved rows, in the same run
-// grouping; then one rounded product and difference per later column of the
-// diagonal block, from the last; then the division.
+// grouping but taken from the last off-block row backward; then one rounded
+// product and difference per later column of the diagonal block, from the
+// last; then the division.
 //
 // Execution.  FP64 on this part issues one warp instruction per 67.5 cycles
 // per SM sub-partition, so a supernode of w columns is far too much work for
@@ -35,20 +36,29 @@
 // warp's:
 //   forward  D(s, i)  rows 32i..32i+31 of s's diagonal block: pull the
 //                     sources' products (in source order), apply the columns
-//                     of tiles 0..i-1 as they are published, solve the
-//                     tile, publish it;
+//                     of tiles 0..i-1, solve the tile;
 //            P(s, o)  32/H off-block rows of s, H lanes per row splitting
 //                     its column runs; the run sums are chained in order
 //                     through shuffles.  Products go to a contribution
 //                     buffer, one slot per (source, off-block row).
 //   transposed O(s, a)  32/H columns' off-block products, x_q updated in
 //                     place;  T(s, i)  tiles from the last, mirror of D.
-// Tasks are listed by supernode level, each supernode's tasks together, and
-// taken in list order through one atomic counter; a task waits only on
-// earlier tasks (bounded waits on per-supernode counters), so the warps
-// that hold the tasks it waits on are running and no wait can deadlock.
-// Counters grow across solves (a solve's targets are multiples of its
-// epoch), so nothing is cleared between solves.
+// Every solved unknown is also stored, the moment it is divided, into a
+// scratch copy of x filled with a sentinel before the launch.  Tiles below
+// it and product tasks poll that copy and use each value as soon as it
+// appears, so a supernode's tiles hand off column by column and its
+// products finish right behind its solve.  Contributions and transposed
+// updates are counted on per-supernode counters that the tiles wait on.
+// Tiles and products form two queues, each listed by supernode level with
+// a supernode's tasks together and taken in list order through its own
+// atomic counter: warp 0 of every block takes tiles, the other warps
+// products, so the dependent chains of the tiles never share an SM
+// sub-partition's FP64 pipe with product work.  A task waits only on tasks
+// earlier in the common order (all waits bounded); the lowest unfinished
+// task is therefore always held by a running warp or next in its queue,
+// and no wait can deadlock.  Counters grow across
+// solves (a solve's targets are multiples of its epoch), so nothing but the
+// scratch copy is reset between solves.
 #include <algorithm>
 #include <climits>
 #include <memory>
@@ -62,26 +72,32 @@ struct SnTask {
   int kind;  // low byte: kind; bits 8.. : target count (forward products)
   int sup, a, b;
 };
+// One task queue: tasks in supernode blocks (block b: tb[b] .. tb[b+1]),
+// and the value its counter reached after the solves so far.
+struct SnQueue {
+  DBuf<SnTask> task;
+  DBuf<int> tb;
+  int ntask = 0;
+  unsigned long long ctr = 0;
+};
 }  // namespace gbsym
 
 struct gbsym_sn_s {
   int n = 0, nsup = 0, nlev = 0, nblev = 0, max_w = 0;
-  int nftask = 0, ntt = 0;  // tasks per right-hand-side group, forward / transposed
   int grid1 = 0, grid8 = 0;  // blocks of the persistent launch, per instantiation
   int groups = 0;            // right-hand-side groups the counters are laid out for
   unsigned long long ef = 0, et = 0;  // solves since the counters were cleared
-  unsigned long long fctr = 0, tctr = 0;  // task-counter values those solves left
   long long ncontrib = 0;
   size_t contrib_k = 0;
   std::vector<int> h_lev_ptr, h_blev_ptr;
-  gbsym::DBuf<int> c0, nr, hf, need_in, n_ot, tg_ptr, tg;
+  gbsym::DBuf<int> c0, nr, hf, need_in, n_ot;
   gbsym::DBuf<long long> rb, vb, coff;
   gbsym::DBuf<int> rows;
   gbsym::DBuf<double> vals;
   gbsym::DBuf<int> pull_ptr, pull_idx;
-  gbsym::DBuf<gbsym::SnTask> ftask, ttask;
-  gbsym::DBuf<int> ftb, ttb, gt_tg;
-  gbsym::DBuf<unsigned long long> flags;  // [fwd ctr, tr ctr] + 4 x nsup x groups
+  gbsym::SnQueue q[4];  // forward tiles, forward products, transposed tiles, transposed products
+  gbsym::DBuf<int> gt_tg;
+  gbsym::DBuf<unsigned long long> flags;  // 4 queue counters + 2 x nsup x groups
   gbsym::DBuf<double> contrib, yscr;
   gbsym::DBuf<int> err;
 };
@@ -97,18 +113,20 @@ constexpr long long kSnWaitCycles = 1ll << 32;  // about two seconds
 enum { kD = 0, kP = 1, kO = 2, kT = 3 };
 
 struct SnView {
-  int n, k, groups, ntask, nblk;
-  const int *c0, *nr, *hsplit, *need_in, *n_ot, *tg_ptr, *tg;
+  int n, k, groups, nblk;
+  int ntask[2];  // per role: tiles, products
+  const int *c0, *nr, *hsplit, *need_in, *n_ot;
   const long long *rb, *vb, *coff;
   const int *rows;
   const double *vals;
   const int *pull_ptr, *pull_idx;
-  const SnTask *task;
-  const int *tb, *gt_tg;
-  unsigned long long *ctr, *done, *in;
+  const SnTask *task[2];
+  const int *tb[2];
+  const int *gt_tg;
+  unsigned long long *ctr[2], *in;
   double *x, *contrib, *y;
   long long ncontrib;
-  unsigned long long epoch, base;
+  unsigned long long epoch, base[2];
   int *err;
 };
 
@@ -207,6 +225,8 @@ __device__ bool sn_wait(const unsigned long long *f, unsigned long long want, in
   }
 }
 
+__device__ __forceinline__ bool lane_zero() { return (threadIdx.x & 31) == 0; }
+
 // After the warp's stores: make them visible before the task is counted.
 __device__ __forceinline__ void sn_fence() {
   __threadfence();
@@ -238,60 +258,96 @@ struct Runs {
 };
 
 // The grouped product sum of one row (forward: entries E[c*estride] and
-// values xb[c]) or one column (transposed: entries E[r] and values
-// xb[idx[r]]), for kr right-hand sides xstride apart.  Lane (rho, h)
-// computes the run sums of runs h, h + H, ...; the running value, which
-// starts at +0, adds them in run order, taken from the H lanes of its row
-// by shuffles.  A run of 8 issues all its loads before its arithmetic.
+// values xb[c], c = 0, 1, ...) or one column (transposed: entries E[p] and
+// values xb[idx[p]] for storage positions p = len-1, len-2, ...), for kr
+// right-hand sides xstride apart.  Lane (rho, h) computes the run sums of
+// runs h, h + H, ...; the running value, which starts at +0, adds them in
+// run order, taken from the H lanes of its row by shuffles.
+//
+// Values are read from the sentinel scratch copy as they are published:
+// forward, the supernode's own unknowns appear in increasing order while
+// its diagonal tiles run; transposed, the ancestors' unknowns appear top
+// down, which is why the transposed runs start from the last off-block row.
+// A run waits (bounded) until all its values are there, so the products
+// finish right behind the solve instead of after it.
 template <int KR, bool TR>
 __device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool act, const double *__restrict__ E,
                                             size_t estride, const int *__restrict__ idx, const double *xb,
-                                            size_t xstride, int kr, double (&acc)[KR]) {
+                                            size_t xstride, int kr, double (&acc)[KR], int *err, bool &failed) {
   const Runs R(len);
 #pragma unroll
   for (int j = 0; j < KR; ++j) acc[j] = 0.0;
+  long long t0 = 0;
   for (int base = 0; base < R.nruns; base += H) {
+    // one lane polls the step's last value in publication order (forward:
+    // its highest column; transposed: its lowest row, the ancestors being
+    // solved top down) before the warp loads the rest
+    {
+      int cl, szl;
+      R.at(min(base + H, R.nruns) - 1, cl, szl);
+      const int el = cl + szl - 1;
+      const size_t xl = TR ? (size_t)__ldg(idx + (len - 1 - el)) : (size_t)el;
+      int ns = 64;
+      for (int j = 0; j < kr && !failed; ++j) {
+        const double *pl = xb + (size_t)j * xstride + xl;
+        while (!__shfl_sync(kFull, lane_zero() ? !unsolved(ld_rlx_f64(pl)) : false, 0)) {
+          if (t0 == 0) t0 = __shfl_sync(kFull, clock64(), 0);
+          __nanosleep(ns);
+          ns = min(2 * ns, 1024);
+          if (__any_sync(kFull, ld_relaxed(err) != 0)) failed = true;
+          if (__shfl_sync(kFull, clock64() - t0 > kSnWaitCycles, 0)) {
+            if (lane_zero()) atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
+            failed = true;
+          }
+          if (failed) break;
+        }
+      }
+    }
     const int r = base + h;
+    const bool has = act && r < R.nruns;
+    int cs = 0, sz = 0;
+    if (has) R.at(r, cs, sz);
+    double m[8];
+    size_t xo[8];
+#pragma unroll
+    for (int b = 0; b < 8; ++b) {
+      const int e = cs + b;
+      const int p = TR ? len - 1 - e : e;
+      m[b] = b < sz ? __ldg(E + (size_t)p * estride) : 0.0;
+      xo[b] = b < sz ? (TR ? (size_t)__ldg(idx + p) : (size_t)p) : 0;
+    }
     double s[KR];
 #pragma unroll
-    for (int j = 0; j < KR; ++j) s[j] = 0.0;
-    if (act && r < R.n8) {
-      const int cs = r << 3;
-      double m[8];
-      size_t xo[8];
+    for (int j = 0; j < KR; ++j) {
+      s[j] = 0.0;
+      if (j < kr) {
+        double xv[8];
+        for (;;) {
+          bool ok = true;
 #pragma unroll
-      for (int b = 0; b < 8; ++b) {
-        m[b] = __ldg(E + (size_t)(cs + b) * estride);
-        xo[b] = TR ? (size_t)__ldg(idx + cs + b) : (size_t)(cs + b);
-      }
-#pragma unroll
-      for (int j = 0; j < KR; ++j)
-        if (j < kr) {
-          double xv[8];
-#pragma unroll
-          for (int b = 0; b < 8; ++b) xv[b] = __ldcg(xb + (size_t)j * xstride + xo[b]);
+          for (int b = 0; b < 8; ++b) {
+            xv[b] = 0.0;
+            if (b < sz) {
+              xv[b] = ld_rlx_f64(xb + (size_t)j * xstride + xo[b]);
+              ok = ok && !unsolved(xv[b]);
+            }
+          }
+          if (__all_sync(kFull, ok) || failed) break;
+          if (t0 == 0) t0 = __shfl_sync(kFull, clock64(), 0);
+          __nanosleep(100);
+          if (__any_sync(kFull, ld_relaxed(err) != 0)) failed = true;
+          if (__shfl_sync(kFull, clock64() - t0 > kSnWaitCycles, 0)) {
+            if ((threadIdx.x & 31) == 0) atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
+            failed = true;
+          }
+        }
+        if (has) {
           double a = xmul(xv[0], m[0]);
 #pragma unroll
-          for (int b = 1; b < 8; ++b) a = xmadd(a, xv[b], m[b]);
+          for (int b = 1; b < 8; ++b)
+            if (b < sz) a = xmadd(a, xv[b], m[b]);
           s[j] = a;
         }
-    } else if (act && r < R.nruns) {
-      int cs, sz;
-      R.at(r, cs, sz);
-      {
-        const double m = __ldg(E + (size_t)cs * estride);
-        const size_t xo = TR ? (size_t)idx[cs] : (size_t)cs;
-#pragma unroll
-        for (int j = 0; j < KR; ++j)
-          if (j < kr) s[j] = xmul(__ldcg(xb + (size_t)j * xstride + xo), m);
-      }
-      for (int b = 1; b < sz; ++b) {
-        const int c = cs + b;
-        const double m = __ldg(E + (size_t)c * estride);
-        const size_t xo = TR ? (size_t)idx[c] : (size_t)c;
-#pragma unroll
-        for (int j = 0; j < KR; ++j)
-          if (j < kr) s[j] = xmadd(s[j], __ldcg(xb + (size_t)j * xstride + xo), m);
       }
     }
     const int top = min(H, R.nruns - base);
@@ -306,27 +362,66 @@ __device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool
   }
 }
 
+// Stages the 32 x 32 entries a tile of supernode rows/columns 32i..
+// applies from tile J (own: J == i, only the strictly triangular part) into
+// S[cc][lane], the entry lane uses at step cc; entries a lane does not use
+// are zero.  Forward: row 32i + lane, column 32J + cc, read with lanes on
+// consecutive rows.  Transposed: column 32i + lane, row 32J + c with
+// c = cnt - 1 - cc, read down each column (lane = row c) for coalescing and
+// written transposed.
+__device__ __forceinline__ void stage_tile(double (*S)[32], const double *__restrict__ M, int ld, int w, int i, int J,
+                                           int cnt, bool fwd, bool own, int lane) {
+  if (fwd) {
+    const int q = (i << 5) + lane;
+#pragma unroll 4
+    for (int cc = 0; cc < 32; ++cc) {
+      const bool use = q < w && cc < cnt && (!own || lane > cc);
+      if (use) cp_async8(&S[cc][lane], M + (size_t)((J << 5) + cc) * ld + q);
+      else S[cc][lane] = 0.0;
+    }
+  } else {
+    const int c = lane;  // the row this lane reads: 32J + c
+#pragma unroll 4
+    for (int qq = 0; qq < 32; ++qq) {
+      const int col = (i << 5) + qq;
+      if (c < cnt) {
+        const bool use = col < w && (!own || qq < c);
+        if (use) cp_async8(&S[cnt - 1 - c][qq], M + (size_t)col * ld + (J << 5) + c);
+        else S[cnt - 1 - c][qq] = 0.0;
+      }
+    }
+    for (int cc = cnt; cc < 32; ++cc) S[cc][lane] = 0.0;
+  }
+  cp_async_commit();
+}
+
 template <int KR>
 __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
-  __shared__ double sm_own[kSnWarps][32][32];
+  __shared__ double sm_own[32][32], sm_app[32][32];  // the tile warp's staging
   const int lane = threadIdx.x & 31;
-  const unsigned long long total = (unsigned long long)V.ntask * V.groups;
+  // Warp 0 of a block takes diagonal tiles, the others products: a
+  // block's warps sit on different SM sub-partitions, so a tile's
+  // dependent chain never shares its FP64 pipe with product work.
+  const int role = (threadIdx.x >> 5) == 0 ? 0 : 1;
+  const int *__restrict__ tb = V.tb[role];
+  const unsigned long long total = (unsigned long long)V.ntask[role] * V.groups;
   for (;;) {
     unsigned long long u = 0;
-    if (lane == 0) u = atomicAdd(V.ctr, 1ull) - V.base;
+    if (lane == 0) u = atomicAdd(V.ctr[role], 1ull) - V.base[role];
     u = __shfl_sync(kFull, u, 0);
     if (u >= total) break;
-    // supernode block b holds groups x (tb[b+1] - tb[b]) task slots
+    // supernode block b holds groups x (tb[b+1] - tb[b]) task slots; the
+    // last block with tb[b] * groups <= u is not empty
     int lo = 0, hi = V.nblk;
     while (hi - lo > 1) {
       const int mid = (lo + hi) >> 1;
-      if ((unsigned long long)V.tb[mid] * V.groups <= u) lo = mid;
+      if ((unsigned long long)tb[mid] * V.groups <= u) lo = mid;
       else hi = mid;
     }
-    const int nb = V.tb[lo + 1] - V.tb[lo];
-    const unsigned long long off = u - (unsigned long long)V.tb[lo] * V.groups;
+    const int nb = tb[lo + 1] - tb[lo];
+    const unsigned long long off = u - (unsigned long long)tb[lo] * V.groups;
     const int g = (int)(off / nb);
-    const SnTask T = V.task[V.tb[lo] + (int)(off % nb)];
+    const SnTask T = V.task[role][tb[lo] + (int)(off % nb)];
     const int kind = T.kind & 0xff, t = T.sup;
     const int j0 = g * KR, kr = min(KR, V.k - j0);
     const int c0 = V.c0[t], w = V.c0[t + 1] - c0, ld = V.nr[t];
@@ -342,18 +437,13 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
       const bool act = q < w;
       const int cnt_own = min(32, w - (i << 5));
       double *const yg = V.y + (size_t)j0 * V.n;
-      // this tile's own entries, in the order the solve uses them, go to
-      // shared memory while the warp waits (forward: row q, columns 32i + c;
-      // transposed: column q, rows 32i + c from the last)
-      double(*so)[32] = sm_own[threadIdx.x >> 5];
-#pragma unroll
-      for (int cc = 0; cc < 32; ++cc) {
-        const int c = fwd ? cc : cnt_own - 1 - cc;
-        const bool upd = act && cc < cnt_own && (fwd ? lane > c : lane < c);
-        if (upd) cp_async8(&so[cc][lane], fwd ? M + (size_t)((i << 5) + c) * ld + q : M + (size_t)q * ld + (i << 5) + c);
-        else so[cc][lane] = 0.0;
-      }
-      cp_async_commit();
+      // this tile's own entries go to shared memory while the warp waits,
+      // so[cc][lane] holding the entry lane uses at step cc.  Forward: row
+      // q, column 32i + cc (lanes read consecutive rows).  Transposed:
+      // column q, row 32i + c with c = cnt - 1 - cc; loaded down each column
+      // (lane = row) so the reads stay coalesced, transposed on the way.
+      double(*so)[32] = sm_own;
+      stage_tile(so, M, ld, w, i, i, cnt_own, fwd, true, lane);
       double d = 1.0, y = 1.0;
       if (act) {
         d = __ldg(M + (size_t)q * ld + q);
@@ -391,11 +481,17 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
         const int J = fwd ? step : nt - 1 - step;
         const int cnt = min(32, w - (J << 5));
         double m[32];
+        if (fwd) {
 #pragma unroll
-        for (int cc = 0; cc < 32; ++cc) {
-          const int c = fwd ? cc : cnt - 1 - cc;
-          m[cc] = (act && cc < cnt) ? __ldg(fwd ? M + (size_t)((J << 5) + c) * ld + q : M + (size_t)q * ld + (J << 5) + c)
-                                    : 0.0;
+          for (int cc = 0; cc < 32; ++cc)
+            m[cc] = (act && cc < cnt) ? __ldg(M + (size_t)((J << 5) + cc) * ld + q) : 0.0;
+        } else {
+          stage_tile(sm_app, M, ld, w, i, J, cnt, false, false, lane);
+          cp_async_wait_all();
+          __syncwarp();
+#pragma unroll
+          for (int cc = 0; cc < 32; ++cc) m[cc] = sm_app[cc][lane];
+          __syncwarp();
         }
         const unsigned inside = cnt == 32 ? kFull : (1u << cnt) - 1u;
         int applied = 0;
@@ -467,18 +563,17 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
         for (int j = 0; j < KR; ++j)
           if (j < kr) xg[(size_t)j * V.n + c0 + q] = v[j];
       }
-      sn_fence();
-      if (lane == 0) red_rel64(V.done + fi);
     } else {
       const int H = V.hsplit[t];
       const int rho = lane / H, h = lane % H;
       double acc[KR];
+      bool failed = false;
       if (kind == kP) {
         // off-block rows w + a + rho: products with the supernode's solution
-        sn_wait(V.done + fi, V.epoch * nt, V.err);
         const int o = T.a + rho;
         const bool act = o < ld - w;
-        grouped_sum<KR, false>(w, H, rho, h, act, M + w + o, ld, nullptr, xg + c0, V.n, kr, acc);
+        grouped_sum<KR, false>(w, H, rho, h, act, M + w + o, ld, nullptr, V.y + (size_t)j0 * V.n + c0, V.n, kr, acc,
+                               V.err, failed);
         if (act && h == 0) {
 #pragma unroll
           for (int j = 0; j < KR; ++j)
@@ -491,15 +586,10 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
         }
       } else {
         // columns a + rho: off-block products with the solved rows below
-        for (int e = V.tg_ptr[t]; e < V.tg_ptr[t + 1]; ++e) {
-          const int s = V.tg[e];
-          const int nts = (V.c0[s + 1] - V.c0[s] + 31) >> 5;
-          sn_wait(V.done + (size_t)s * V.groups + g, V.epoch * nts, V.err);
-        }
         const int col = T.a + rho;
         const bool act = col < w;
-        grouped_sum<KR, true>(ld - w, H, rho, h, act, M + (size_t)col * ld + w, 1, V.rows + V.rb[t] + w, xg, V.n,
-                              kr, acc);
+        grouped_sum<KR, true>(ld - w, H, rho, h, act, M + (size_t)col * ld + w, 1, V.rows + V.rb[t] + w,
+                              V.y + (size_t)j0 * V.n, V.n, kr, acc, V.err, failed);
         if (act && h == 0) {
 #pragma unroll
           for (int j = 0; j < KR; ++j)
@@ -611,25 +701,19 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
   t->nblev = (int)t->h_blev_ptr.size() - 1;
   // task lists, by supernode level.  Lanes per row (forward products) and
   // per column (transposed) live in one array, the transposed half second.
-  std::vector<int> hs(2 * nsup), need_in(nsup, 0), n_ot(nsup, 0), tg_ptr(nsup + 1, 0), tg, gt_tg;
-  std::vector<SnTask> ft, tt;
-  std::vector<int> ftb(nsup + 1), ttb(nsup + 1);
+  std::vector<int> hs(2 * nsup), need_in(nsup, 0), n_ot(nsup, 0), gt_tg;
   for (int q = 0; q < nsup; ++q) {
     const int w = c0[q + 1] - c0[q];
     hs[q] = split_for(w);
     hs[nsup + q] = split_for(nr[q] - w);
-    int prev = -1;
-    for (int k = w; k < nr[q]; ++k) {
-      const int u = col2sup[Li[rb[q] + k]];
-      if (u != prev) tg.push_back(u);
-      prev = u;
-    }
-    tg_ptr[q + 1] = (int)tg.size();
   }
+  std::vector<SnTask> L[4];  // forward tiles, forward products, transposed tiles, transposed products
+  std::vector<int> tbs[4];
   for (int b = 0; b < nsup; ++b) {
     const int q = lset[b], w = c0[q + 1] - c0[q], nb = nr[q] - w, nt = (w + 31) / 32;
-    ftb[b] = (int)ft.size();
-    for (int i = 0; i < nt; ++i) ft.push_back({kD, q, i, 0});
+    tbs[0].push_back((int)L[0].size());
+    tbs[1].push_back((int)L[1].size());
+    for (int i = 0; i < nt; ++i) L[0].push_back({kD, q, i, 0});
     const int R = 32 / hs[q];
     for (int o = 0; o < nb; o += R) {
       const int start = (int)gt_tg.size();
@@ -642,22 +726,26 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
         }
         prev = u;
       }
-      ft.push_back({kP | (((int)gt_tg.size() - start) << 8), q, o, start});
+      L[1].push_back({kP | (((int)gt_tg.size() - start) << 8), q, o, start});
     }
   }
-  ftb[nsup] = (int)ft.size();
   for (int b = 0; b < nsup; ++b) {
     const int q = bset[b], w = c0[q + 1] - c0[q], nb = nr[q] - w, nt = (w + 31) / 32;
-    ttb[b] = (int)tt.size();
+    tbs[2].push_back((int)L[2].size());
+    tbs[3].push_back((int)L[3].size());
     if (nb > 0) {
       const int R = 32 / hs[nsup + q];
-      for (int a = 0; a < w; a += R, ++n_ot[q]) tt.push_back({kO, q, a, 0});
+      for (int a = 0; a < w; a += R, ++n_ot[q]) L[3].push_back({kO, q, a, 0});
     }
-    for (int i = nt - 1; i >= 0; --i) tt.push_back({kT, q, i, 0});
+    for (int i = nt - 1; i >= 0; --i) L[2].push_back({kT, q, i, 0});
   }
-  ttb[nsup] = (int)tt.size();
-  t->nftask = (int)ft.size();
-  t->ntt = (int)tt.size();
+  for (int l = 0; l < 4; ++l) {
+    tbs[l].push_back((int)L[l].size());
+    t->q[l].ntask = (int)L[l].size();
+    if (L[l].empty()) L[l].push_back({kD, 0, 0, 0});  // never taken: the queue is empty
+    upload(t->q[l].task, L[l].data(), L[l].size(), false, s);
+    upload(t->q[l].tb, tbs[l].data(), tbs[l].size(), false, s);
+  }
   upload(t->c0, c0.data(), c0.size(), false, s);
   upload(t->nr, nr.data(), nr.size(), false, s);
   upload(t->rb, rb.data(), rb.size(), false, s);
@@ -670,15 +758,8 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
   upload(t->hf, hs.data(), hs.size(), false, s);
   upload(t->need_in, need_in.data(), need_in.size(), false, s);
   upload(t->n_ot, n_ot.data(), n_ot.size(), false, s);
-  upload(t->tg_ptr, tg_ptr.data(), tg_ptr.size(), false, s);
-  if (tg.empty()) tg.push_back(0);
-  upload(t->tg, tg.data(), tg.size(), false, s);
   if (gt_tg.empty()) gt_tg.push_back(0);
   upload(t->gt_tg, gt_tg.data(), gt_tg.size(), false, s);
-  upload(t->ftask, ft.data(), ft.size(), false, s);
-  upload(t->ttask, tt.data(), tt.size(), false, s);
-  upload(t->ftb, ftb.data(), ftb.size(), false, s);
-  upload(t->ttb, ttb.data(), ttb.size(), false, s);
   t->err.alloc(2);
   GB_CUDA(cudaMemsetAsync(t->err.p, 0, 2 * sizeof(int), s));
   t->grid1 = sn_grid<1>();
@@ -693,10 +774,11 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
   const int G = (k + KR - 1) / KR;
   const size_t per = (size_t)t->nsup * G;
   if (G != t->groups) {
-    t->flags.alloc(2 + 4 * per);
+    t->flags.alloc(4 + 2 * per);
     GB_CUDA(cudaMemsetAsync(t->flags.p, 0, t->flags.n * sizeof(unsigned long long), s));
     t->groups = G;
-    t->ef = t->et = t->fctr = t->tctr = 0;
+    t->ef = t->et = 0;
+    for (auto &qq : t->q) qq.ctr = 0;
   }
   if (!transposed && t->ncontrib > 0 && t->contrib_k < (size_t)k) {
     t->contrib.alloc((size_t)t->ncontrib * k);
@@ -705,7 +787,6 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
   if (t->yscr.n < (size_t)t->n * k) t->yscr.alloc((size_t)t->n * k);
   fill_sentinel(t->yscr.p, (size_t)t->n * k * sizeof(double), s);
   const int grid = KR == 1 ? t->grid1 : t->grid8;
-  const unsigned long long nwarps = (unsigned long long)grid * kSnWarps;
   SnView V{};
   V.n = t->n;
   V.k = k;
@@ -716,8 +797,6 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
   V.hsplit = t->hf.p + (transposed ? t->nsup : 0);
   V.need_in = t->need_in.p;
   V.n_ot = t->n_ot.p;
-  V.tg_ptr = t->tg_ptr.p;
-  V.tg = t->tg.p;
   V.rb = t->rb.p;
   V.vb = t->vb.p;
   V.coff = t->coff.p;
@@ -732,27 +811,19 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
   V.ncontrib = t->ncontrib;
   V.err = t->err.p;
   unsigned long long *f = t->flags.p;
-  if (!transposed) {
-    V.ntask = t->nftask;
-    V.task = t->ftask.p;
-    V.tb = t->ftb.p;
-    V.ctr = f;
-    V.done = f + 2;
-    V.in = f + 2 + per;
-    V.base = t->fctr;
-    t->fctr += (unsigned long long)t->nftask * G + nwarps;  // every warp takes one slot past the end
-    V.epoch = ++t->ef;
-  } else {
-    V.ntask = t->ntt;
-    V.task = t->ttask.p;
-    V.tb = t->ttb.p;
-    V.ctr = f + 1;
-    V.done = f + 2 + 2 * per;
-    V.in = f + 2 + 3 * per;
-    V.base = t->tctr;
-    t->tctr += (unsigned long long)t->ntt * G + nwarps;
-    V.epoch = ++t->et;
+  const int q0 = transposed ? 2 : 0;
+  for (int role = 0; role < 2; ++role) {
+    SnQueue &Q = t->q[q0 + role];
+    V.ntask[role] = Q.ntask;
+    V.task[role] = Q.task.p;
+    V.tb[role] = Q.tb.p;
+    V.ctr[role] = f + q0 + role;
+    V.base[role] = Q.ctr;
+    // every warp of the role takes one slot past the end
+    Q.ctr += (unsigned long long)Q.ntask * G + (unsigned long long)grid * (role == 0 ? 1 : kSnWarps - 1);
   }
+  V.in = f + 4 + (transposed ? per : 0);
+  V.epoch = transposed ? ++t->et : ++t->ef;
   if (KR == 1) k_sn<1><<<grid, kSnWarps * 32, 0, s>>>(V);
   else k_sn<8><<<grid, kSnWarps * 32, 0, s>>>(V);
   check_launch();
