@@ -50,6 +50,8 @@ def parse():
     ap.add_argument("--rhs", type=int, default=64)
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--extras-only", action="store_true")
+    ap.add_argument("--supernodal-grid", type=int, default=0,
+                    help="run only the supernodal-solve extra, on a G^3 grid's factor (profiling runs)")
     ap.add_argument("--exec", default="auto",
                     choices=["auto", "levelset", "syncfree", "oneblock", "persistent", "cluster", "partitioned"],
                     help="force one executor instead of autotuning (profiling runs)")
@@ -62,9 +64,11 @@ def algorithmic_bytes(nnz_l, n, k, vbytes=8, sbytes=8):
     return (vbytes + 4) * nnz_l + 4 * (n + 1) + 2 * sbytes * k * n
 
 
-# FP64 throughput of this machine's GB300 (dependent-free DFMA stream, all SMs):
-# 502 G operations/s, measured by a microbenchmark during development.  On
-# this part the FP64 pipe, not HBM, bounds an FP64 triangular solve.
+# FP64 throughput of this GB300 (dependent-free DFMA stream, all SMs): 597 G
+# operations/s (502 G for separate multiplies and adds), measured by a
+# microbenchmark during development.  On this part the FP64 pipe, not HBM,
+# bounds an FP64 triangular solve; the exact kernels issue every rounded
+# operation as an FMA.
 FP64_PEAK_GOPS = 597.0
 
 
@@ -323,6 +327,85 @@ def bench_spmv(dev, stream, flush):
     return out
 
 
+def bench_supernodal(dev, stream, flush, grid=64):
+    """ParSy's supernodal solves (blockedLsolve / blockedLTsolve and their
+    multi-RHS forms) on the supernodal Cholesky structure of the C2 operator
+    (3D 7-point Laplacian 64^3) in geometric nested-dissection order:
+    separators and leaf boxes of at most 64 nodes as supernodes, random
+    diagonally dominant values.  FP64 ops count a multiply and an add per
+    stored lower entry and three for each division; bytes are the used
+    lower-block values, the row lists and x read and written once."""
+    import torch
+    from sympiler_gb300 import matgen as mg
+    from sympiler_gb300 import sym_lib
+    from sympiler_gb300.plans import SupernodalPlan
+    S = mg.nd_supernodal(grid, grid, grid, leaf=64, rng=np.random.default_rng(1))
+    w = np.diff(S.sup2col).astype(np.int64)
+    nr = (S.Li_ptr[S.sup2col[1:]] - S.Li_ptr[S.sup2col[:-1]]).astype(np.int64)
+    used_off = int(np.sum(w * (w - 1) // 2 + w * (nr - w)))
+    t0 = time.perf_counter()
+    P = SupernodalPlan(S)
+    torch.cuda.synchronize()
+    plan_s = time.perf_counter() - t0
+    f_lev, t_lev = P.levels()
+    out = {"workload": "supernodal Cholesky structure of the 3D 7-pt Laplacian %d^3, nested dissection" % grid,
+           "n": S.n, "supernodes": S.nsup, "max_width": int(w.max()), "stored_values": int(len(S.Lx)),
+           "used_offdiag": used_off, "levels": [f_lev, t_lev], "plan_s": plan_s,
+           "gpu_launches_per_solve": 2}
+    rng = np.random.default_rng(2)
+    for k in (1, 64):
+        X0 = torch.from_numpy(rng.standard_normal((k, S.n))).to(dev)
+        X = X0.clone()
+        ops = k * (2 * used_off + 3 * S.n)
+        byt = 8 * (used_off + S.n) + 4 * int(nr.sum()) + 16 * S.n * k
+        for tr in (False, True):
+            def run():
+                X.copy_(X0)
+                P.solve(X if k > 1 else X[0], transposed=tr)
+            run()
+            P.check()
+            t = _time(run, 5 if k == 1 else 3, stream, flush)
+            P.check()
+            key = "%s_k%d" % ("transposed" if tr else "forward", k)
+            out[key] = {"ms": t * 1e3, "fp64_gops": ops / t / 1e9, "fp64_frac": ops / t / 1e9 / FP64_PEAK_GOPS,
+                        "gbs": byt / t / 1e9}
+    # end to end with host buffers, factor resident: H2D, solve, D2H
+    hx = torch.from_numpy(rng.standard_normal(S.n)).pin_memory()
+    dx = torch.empty(S.n, dtype=torch.float64, device=dev)
+    hy = torch.empty(S.n, dtype=torch.float64).pin_memory()
+
+    def e2e():
+        dx.copy_(hx, non_blocking=True)
+        P.solve(dx)
+        hy.copy_(dx, non_blocking=True)
+    e2e()
+    out["forward_k1_e2e_ms"] = _time(e2e, 5, stream) * 1e3
+    # the reference-facing drop-in: builds its plan, uploads the factor, solves
+    xb = np.random.default_rng(3).standard_normal(S.n)
+    x = xb.copy()
+    t0 = time.perf_counter()
+    assert sym_lib.parsy.blockedLsolve(S, x) == 1
+    out["dropin_blockedLsolve_s"] = time.perf_counter() - t0
+    # the reference's own serial blockedLsolve, compiled from its sources
+    # (CPU baseline leg only)
+    try:
+        import oracle
+        r = oracle.ref()
+        kind = "reference" if r is not None else "port"
+        xr = xb.copy()
+        t0 = time.perf_counter()
+        (r.blocked_lsolve if r is not None else oracle.orc().blocked_lsolve)(S, xr)
+        cpu = time.perf_counter() - t0
+        out["cpu_reference_blockedLsolve"] = {"s": cpu, "cores": 1, "kind": kind,
+                                              "speedup_device": cpu / (out["forward_k1"]["ms"] / 1e3),
+                                              "speedup_e2e": cpu / (out["forward_k1_e2e_ms"] / 1e3),
+                                              "bit_exact": bool(np.array_equal(xr, x))}
+    except Exception as ex:  # the baseline must not hide the GPU numbers
+        out["cpu_reference_blockedLsolve"] = {"error": str(ex)}
+    del P
+    return out
+
+
 def bench_adjoint(dev, stream, flush, g=1024, k=32):
     """Forward X = L^{-1} B and the reverse pass (L^T solve + value gradient)
     on the IC0 factor of the 1024^2 anisotropic variable-coefficient Poisson
@@ -388,6 +471,12 @@ def main():
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
+    if args.supernodal_grid:
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+        out = bench_supernodal(dev, torch.cuda.current_stream(), flush, grid=args.supernodal_grid)
+        if rank == 0:
+            print(json.dumps({"extras": {"supernodal_nd": out}}), flush=True)
+        return
 
     from sympiler_gb300 import matgen as mg
     from sympiler_gb300 import plans
@@ -645,6 +734,7 @@ def main():
         extras["batch_c4"] = bench_batch(dev, stream, flush)
         extras["adjoint_c5"] = bench_adjoint(dev, stream, flush)
         extras["spmv"] = bench_spmv(dev, stream, flush)
+        extras["supernodal_c2_nd"] = bench_supernodal(dev, stream, flush)
         result["extras"] = extras
     if rank == 0:
         if not args.extras_only:

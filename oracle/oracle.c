@@ -624,35 +624,45 @@ static void blk_diag_solve(int ld, int w, const double *M, double *rhs) {
   }
 }
 
-/* out[k] = dot of row k of the nrow x ncol block M (leading dimension ld)
- * with vec, in the reference's grouping: column runs of 8, then 4, then 1;
- * each run's products summed left to right, then added to the running
- * value, which starts at +0 (BLAS.cpp:123-185). */
-static double blk_row_dot(int ld, int ncol, const double *M, int k, const double *vec) {
-  double acc = 0.0;
+/* out[k] = the dot of off-block row w + k of the ld x ncol block M
+ * (column-major) with vec, for the nrow = ld - w rows below a w-row
+ * diagonal block, in the reference's grouping: column runs of 8 while 8
+ * remain, then 4, then 1; each run's products summed left to right, then
+ * added to the running value, which starts at +0.  Runs are outermost so
+ * that every pass walks the rows contiguously, as dmatvec_blas does
+ * (BLAS.cpp:123-185); each row's arithmetic is unchanged by that. */
+static void blk_rows_dot(int ld, int ncol, const double *M, int nrow, const double *vec, double *out) {
+  const int w = ld - nrow;
+  for (int k = 0; k < nrow; ++k) out[k] = 0.0;
   int fc = 0;
   while (fc < ncol - 7) {
-    double s = vec[fc] * M[(size_t)fc * ld + k];
-    for (int b = 1; b < 8; ++b) s = s + vec[fc + b] * M[(size_t)(fc + b) * ld + k];
-    acc = acc + s;
+    const double *m0 = M + (size_t)fc * ld + w;
+    for (int k = 0; k < nrow; ++k) {
+      double s = vec[fc] * m0[k];
+      for (int b = 1; b < 8; ++b) s = s + vec[fc + b] * m0[(size_t)b * ld + k];
+      out[k] = out[k] + s;
+    }
     fc += 8;
   }
   while (fc < ncol - 3) {
-    double s = vec[fc] * M[(size_t)fc * ld + k];
-    for (int b = 1; b < 4; ++b) s = s + vec[fc + b] * M[(size_t)(fc + b) * ld + k];
-    acc = acc + s;
+    const double *m0 = M + (size_t)fc * ld + w;
+    for (int k = 0; k < nrow; ++k) {
+      double s = vec[fc] * m0[k];
+      for (int b = 1; b < 4; ++b) s = s + vec[fc + b] * m0[(size_t)b * ld + k];
+      out[k] = out[k] + s;
+    }
     fc += 4;
   }
   while (fc < ncol) {
-    acc = acc + vec[fc] * M[(size_t)fc * ld + k];
+    const double *m0 = M + (size_t)fc * ld + w;
+    for (int k = 0; k < nrow; ++k) out[k] = out[k] + vec[fc] * m0[k];
     fc += 1;
   }
-  return acc;
 }
 
 /* The off-block part of column q in the transposed solve: sum over the
  * nb off-block rows of col[r] * x[rows[r]], taken from the LAST row
- * backward and grouped as blk_row_dot groups a row: runs of 8 while 8
+ * backward and grouped as blk_rows_dot groups a row: runs of 8 while 8
  * remain, then 4, then 1; each run summed in that order, then added to a
  * running value that starts at +0.  This order is this library's own (its
  * GPU solve consumes the ancestors' unknowns as they appear, top down): the
@@ -689,6 +699,13 @@ static double blk_col_dot(int nb, const double *col, const int *rows, const doub
 void orc_blocked_lsolve(int n, const size_t *Lp, const int *Li, const double *Lx,
                         const size_t *Li_ptr, const int *sup2col, int supNo,
                         double *x, int nrhs) {
+  int maxoff = 1;
+  for (int s = 0; s < supNo; ++s) {
+    const int w = sup2col[s + 1] - sup2col[s];
+    const int nr = (int)(Li_ptr[sup2col[s + 1]] - Li_ptr[sup2col[s]]);
+    if (nr - w > maxoff) maxoff = nr - w;
+  }
+  double *tmp = (double *)malloc(sizeof(double) * (size_t)maxoff);
   for (int j = 0; j < nrhs; ++j) {
     double *xj = x + (size_t)j * n;
     for (int s = 0; s < supNo; ++s) {
@@ -696,13 +713,14 @@ void orc_blocked_lsolve(int n, const size_t *Lp, const int *Li, const double *Lx
       const int nr = (int)(Li_ptr[c1] - Li_ptr[c0]);
       const double *M = Lx + Lp[c0];
       blk_diag_solve(nr, w, M, xj + c0);
+      blk_rows_dot(nr, w, M, nr - w, xj + c0, tmp);
       for (int k = w; k < nr; ++k) {
-        const double c = blk_row_dot(nr, w, M, k, xj + c0);
         const int r = Li[Li_ptr[c0] + k];
-        xj[r] = xj[r] - c;
+        xj[r] = xj[r] - tmp[k - w];
       }
     }
   }
+  free(tmp);
 }
 
 void orc_blocked_ltsolve(int n, const size_t *Lp, const int *Li, const double *Lx,
@@ -716,10 +734,14 @@ void orc_blocked_ltsolve(int n, const size_t *Lp, const int *Li, const double *L
       const double *M = Lx + Lp[c0];
       for (int q = 0; q < w; ++q)
         xj[c0 + q] = xj[c0 + q] - blk_col_dot(nr - w, M + (size_t)q * nr + w, Li + Li_ptr[c0] + w, xj);
-      for (int q = w - 1; q >= 0; --q) {
-        const double v = xj[c0 + q] / M[(size_t)q * nr + q];
-        xj[c0 + q] = v;
-        for (int i = 0; i < q; ++i) xj[c0 + i] = xj[c0 + i] - M[(size_t)i * nr + q] * v;
+      /* the diagonal block's transpose backward: unknown i subtracts
+       * L[q, i] x_q for q from the last down to i + 1, then divides (the
+       * solved x_q are final when i is reached; column i is contiguous) */
+      for (int i = w - 1; i >= 0; --i) {
+        const double *Mi = M + (size_t)i * nr;
+        double v = xj[c0 + i];
+        for (int q = w - 1; q > i; --q) v = v - Mi[q] * xj[c0 + q];
+        xj[c0 + i] = v / Mi[i];
       }
     }
   }
