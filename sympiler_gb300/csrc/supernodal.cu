@@ -84,7 +84,7 @@ struct SnQueue {
 
 struct gbsym_sn_s {
   int n = 0, nsup = 0, nlev = 0, nblev = 0, max_w = 0;
-  int grid1 = 0, grid8 = 0;  // blocks of the persistent launch, per instantiation
+  int grid = 0;              // blocks of the persistent launch
   int groups = 0;            // right-hand-side groups the counters are laid out for
   unsigned long long ef = 0, et = 0;  // solves since the counters were cleared
   long long ncontrib = 0;
@@ -108,6 +108,12 @@ void fill_sentinel(void *y, size_t bytes, cudaStream_t s);  // exec_syncfree.cu
 namespace {
 
 constexpr int kSnWarps = 4;
+// Right-hand sides per task.  Each right-hand side is its own pipeline of
+// tasks; measured on the 64^3 nested-dissection factor, one per task beat
+// 2, 4 and 8 per task at 8 and at 64 right-hand sides (9.2 / 66 ms against
+// 11.3 / 71, 16.2 / 84 and 25.3 / 96 ms forward): fewer registers keep more
+// warps resident and the independent pipelines overlap.
+constexpr int kSnRhs = 1;
 constexpr unsigned kFull = 0xffffffffu;
 constexpr long long kSnWaitCycles = 1ll << 32;  // about two seconds
 enum { kD = 0, kP = 1, kO = 2, kT = 3 };
@@ -762,16 +768,14 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
   upload(t->gt_tg, gt_tg.data(), gt_tg.size(), false, s);
   t->err.alloc(2);
   GB_CUDA(cudaMemsetAsync(t->err.p, 0, 2 * sizeof(int), s));
-  t->grid1 = sn_grid<1>();
-  t->grid8 = sn_grid<8>();
+  t->grid = sn_grid<kSnRhs>();
   GB_CUDA(cudaStreamSynchronize(s));
   return t.release();
 }
 
 void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) {
   if (t->n == 0 || k == 0) return;
-  const int KR = k == 1 ? 1 : 8;
-  const int G = (k + KR - 1) / KR;
+  const int G = (k + kSnRhs - 1) / kSnRhs;
   const size_t per = (size_t)t->nsup * G;
   if (G != t->groups) {
     t->flags.alloc(4 + 2 * per);
@@ -786,7 +790,7 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
   }
   if (t->yscr.n < (size_t)t->n * k) t->yscr.alloc((size_t)t->n * k);
   fill_sentinel(t->yscr.p, (size_t)t->n * k * sizeof(double), s);
-  const int grid = KR == 1 ? t->grid1 : t->grid8;
+  const int grid = t->grid;
   SnView V{};
   V.n = t->n;
   V.k = k;
@@ -824,8 +828,7 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
   }
   V.in = f + 4 + (transposed ? per : 0);
   V.epoch = transposed ? ++t->et : ++t->ef;
-  if (KR == 1) k_sn<1><<<grid, kSnWarps * 32, 0, s>>>(V);
-  else k_sn<8><<<grid, kSnWarps * 32, 0, s>>>(V);
+  k_sn<kSnRhs><<<grid, kSnWarps * 32, 0, s>>>(V);
   check_launch();
 }
 
