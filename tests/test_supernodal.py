@@ -222,6 +222,38 @@ def test_gpu_supernodal_plan_many_rhs_and_wide_supernodes(gpu, orc):
 
 
 @pytest.mark.gpu
+def test_gpu_supernodal_degenerate_shapes(gpu, orc):
+    """A block-diagonal factor (no off-block rows: no products, no
+    contributions), one dense supernode of 63 columns (two tiles), and zero
+    right-hand sides; forward and transposed against the restatement."""
+    import torch
+    from sympiler_gb300.plans import SupernodalPlan
+    cases = [mg.random_supernodal(40, 50, 0, np.random.default_rng(2)),
+             mg.random_supernodal(1, 77, 0, np.random.default_rng(3))]
+    assert np.diff(cases[1].sup2col)[0] == 63
+    for S in cases:
+        P = SupernodalPlan(S)
+        for k in (1, 4):
+            X = np.random.default_rng(k).standard_normal((k, S.n))
+            for transposed in (False, True):
+                W = X.copy()
+                (orc.blocked_ltsolve if transposed else orc.blocked_lsolve)(S, W if k > 1 else W[0])
+                Xd = torch.from_numpy(X.copy()).cuda()
+                P.solve(Xd if k > 1 else Xd[0], transposed=transposed)
+                P.check()
+                assert np.array_equal(Xd.cpu().numpy(), W), (S.nsup, k, transposed)
+        Xd = torch.zeros((0, S.n), dtype=torch.float64, device="cuda")
+        P.solve(Xd)  # no right-hand sides: nothing to do
+        P.check()
+    E = mg.Supernodal(0, 0, np.zeros(1, np.uint64), np.zeros(0, np.int32), np.zeros(0), np.zeros(1, np.uint64),
+                      np.zeros(0, np.int32), np.zeros(1, np.int32))
+    P = SupernodalPlan(E)
+    assert P.levels() == (0, 0)
+    P.solve(torch.zeros(0, dtype=torch.float64, device="cuda"))
+    P.check()
+
+
+@pytest.mark.gpu
 def test_gpu_supernodal_rejects_malformed_storage(gpu):
     from sympiler_gb300 import sym_lib
     from sympiler_gb300._lib import ERR_BAD_MATRIX as GBSYM_ERR_BAD_MATRIX, lib
