@@ -12,22 +12,31 @@
 
 namespace gbsym {
 
-// One warp per row i of L (CSR, diagonal last).  Lanes hold G_B[i, :] and
-// reduce the k-term products of each stored entry.
+// One thread per row i of L (CSR, diagonal last), each stored entry's
+// k-term product in four interleaved partial sums.  Lanes across rows keep
+// every FP64 instruction full: a lane-per-right-hand-side layout needs a
+// five-step shuffle reduction per entry, six warp FP64 instructions for
+// one instruction's worth of products, and this part's FP64 issue rate is
+// the bound.  G_B's row is re-read from L1 for each entry.
 __global__ void __launch_bounds__(256)
 k_value_grad(int n, const int *__restrict__ Lp, const int *__restrict__ Li,
              const double *__restrict__ X, const double *__restrict__ GB, int k,
              double *__restrict__ grad) {
-  const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double *gi = GB + (size_t)i * k;
   for (int e = Lp[i]; e < Lp[i + 1]; ++e) {
     const double *xj = X + (size_t)Li[e] * k;
-    double s = 0.0;
-    for (int r = lane; r < k; r += 32) s += gi[r] * xj[r];
-    for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (lane == 0) grad[e] = -s;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int r = 0;
+    for (; r + 4 <= k; r += 4) {
+      s0 = __fma_rn(__ldg(gi + r), __ldg(xj + r), s0);
+      s1 = __fma_rn(__ldg(gi + r + 1), __ldg(xj + r + 1), s1);
+      s2 = __fma_rn(__ldg(gi + r + 2), __ldg(xj + r + 2), s2);
+      s3 = __fma_rn(__ldg(gi + r + 3), __ldg(xj + r + 3), s3);
+    }
+    for (; r < k; ++r) s0 = __fma_rn(__ldg(gi + r), __ldg(xj + r), s0);
+    grad[e] = -((s0 + s1) + (s2 + s3));
   }
 }
 
@@ -37,7 +46,7 @@ void tri_adjoint(gbsym_tri_s *Lt, int n, const int *Lp, const int *Li, const dou
   GB_CHECK(kind_is_upper(Lt->kind), GBSYM_ERR_UNSUPPORTED);
   if (n == 0) return;
   tri_solve_rowmajor(Lt, g, nullptr, k, GBSYM_F64, s);
-  k_value_grad<<<div_up(n, 8), 256, 0, s>>>(n, Lp, Li, X, g, k, grad);
+  k_value_grad<<<div_up(n, 256), 256, 0, s>>>(n, Lp, Li, X, g, k, grad);
   check_launch();
 }
 
