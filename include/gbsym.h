@@ -264,6 +264,41 @@ int gbsym_parsy_H2LeveledBlockedLTsolve_mrhs(
     int *levelPtr, int *levelSet, int parts, int *parPtr, int *partition,
     int chunk, int max_col);
 
+/* The supernodal LL^T solve phases: the forward solve, then the transposed
+ * one, on one resident plan; x (n x n_rhs, column-major) in place.  void,
+ * as in the reference: the status is in gbsym_last_error().  The
+ * scheduled forms validate the LBC schedule for both directions (the
+ * transposed solve walks it backward).  Replace parsy::
+ * solve_phase_ll_blocked, _nrhs, _parallel and _parallel_nrhs
+ * (sparse_blas/parsy/linear_solver/solve_phase.cpp:39-94). */
+void gbsym_parsy_solve_phase_ll_blocked(size_t n, double *x, int *col2sup,
+                                        int *sup2col, size_t *newCol,
+                                        int *newRow, double *newVal,
+                                        size_t *rowP, size_t nBlocks, int nnz);
+void gbsym_parsy_solve_phase_ll_blocked_nrhs(size_t n, double *x, int n_rhs,
+                                             int *col2sup, int *sup2col,
+                                             size_t *newCol, int *newRow,
+                                             double *newVal, size_t *rowP,
+                                             size_t nBlocks, int nnz,
+                                             int max_col);
+void gbsym_parsy_solve_phase_ll_blocked_parallel(
+    size_t n, double *x, int *col2sup, int *sup2col, size_t *newCol,
+    int *newRow, double *newVal, size_t *rowP, size_t nBlocks, int nnz,
+    int levels, int *levelPtr, int *levelSet, int parts, int *parPtr,
+    int *partition, int chunk);
+void gbsym_parsy_solve_phase_ll_blocked_parallel_nrhs(
+    size_t n, double *x, int n_rhs, int *col2sup, int *sup2col,
+    size_t *newCol, int *newRow, double *newVal, size_t *rowP,
+    size_t nBlocks, int nnz, int levels, int *levelPtr, int *levelSet,
+    int parts, int *parPtr, int *partition, int chunk, int max_col);
+/* The LDL^T solve phase with a diagonal D: forward solve, x[i] /= d[i]
+ * (IEEE division, as parsy::scale_vec_vec), transposed solve.  Replaces
+ * parsy::solve_phase_ldl (solve_phase.cpp:96-112). */
+void gbsym_parsy_solve_phase_ldl(size_t n, double *d_val, double *x,
+                                 int *col2sup, int *sup2col, size_t *newCol,
+                                 int *newRow, double *newVal, size_t *rowP,
+                                 size_t nBlocks, int nnz);
+
 /* Supernodal plan: the factor resident on the GPU with its solve task
  * lists (host arrays in).  gbsym_sn_solve works on device memory, x
  * column-major n x k, forward (transposed = 0) or L^T (transposed = 1);

@@ -228,6 +228,36 @@ inline int H2LeveledBlockedLTsolve_mrhs(int n, size_t *Lp, int *Li, double *Lx, 
                                                   levels, levelPtr, levelSet, parts, parPtr, partition, chunk,
                                                   max_col);
 }
+// linear_solver/solve_phase.h:35-62
+inline void solve_phase_ll_blocked(size_t n, double *x, int *col2sup, int *sup2col, size_t *newCol, int *newRow,
+                                   double *newVal, size_t *rowP, size_t nBlocks, int nnz) {
+  gbsym_parsy_solve_phase_ll_blocked(n, x, col2sup, sup2col, newCol, newRow, newVal, rowP, nBlocks, nnz);
+}
+inline void solve_phase_ll_blocked_nrhs(size_t n, double *x, int n_rhs, int *col2sup, int *sup2col, size_t *newCol,
+                                        int *newRow, double *newVal, size_t *rowP, size_t nBlocks, int nnz,
+                                        int max_col) {
+  gbsym_parsy_solve_phase_ll_blocked_nrhs(n, x, n_rhs, col2sup, sup2col, newCol, newRow, newVal, rowP, nBlocks, nnz,
+                                          max_col);
+}
+inline void solve_phase_ll_blocked_parallel(size_t n, double *x, int *col2sup, int *sup2col, size_t *newCol,
+                                            int *newRow, double *newVal, size_t *rowP, size_t nBlocks, int nnz,
+                                            int levels, int *levelPtr, int *levelSet, int parts, int *parPtr,
+                                            int *partition, int chunk) {
+  gbsym_parsy_solve_phase_ll_blocked_parallel(n, x, col2sup, sup2col, newCol, newRow, newVal, rowP, nBlocks, nnz,
+                                              levels, levelPtr, levelSet, parts, parPtr, partition, chunk);
+}
+inline void solve_phase_ll_blocked_parallel_nrhs(size_t n, double *x, int n_rhs, int *col2sup, int *sup2col,
+                                                 size_t *newCol, int *newRow, double *newVal, size_t *rowP,
+                                                 size_t nBlocks, int nnz, int levels, int *levelPtr, int *levelSet,
+                                                 int parts, int *parPtr, int *partition, int chunk, int max_col) {
+  gbsym_parsy_solve_phase_ll_blocked_parallel_nrhs(n, x, n_rhs, col2sup, sup2col, newCol, newRow, newVal, rowP,
+                                                   nBlocks, nnz, levels, levelPtr, levelSet, parts, parPtr,
+                                                   partition, chunk, max_col);
+}
+inline void solve_phase_ldl(size_t n, double *d_val, double *x, int *col2sup, int *sup2col, size_t *newCol,
+                            int *newRow, double *newVal, size_t *rowP, size_t nBlocks, int nnz) {
+  gbsym_parsy_solve_phase_ldl(n, d_val, x, col2sup, sup2col, newCol, newRow, newVal, rowP, nBlocks, nnz);
+}
 // mgmres.hpp:41
 inline void lus_cr(int n, int nz_num, int ia[], int ja[], double l[], int ua[], double r[],
                    double z[]) {

@@ -11,7 +11,7 @@ import os
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgbsym.so")
 
-_int, _dbl, _vp, _ull, _ll = C.c_int, C.c_double, C.c_void_p, C.c_ulonglong, C.c_longlong
+_int, _dbl, _vp, _ull, _ll, _sz = C.c_int, C.c_double, C.c_void_p, C.c_ulonglong, C.c_longlong, C.c_size_t
 _pi = C.POINTER(C.c_int)
 _pd = C.POINTER(C.c_double)
 _ppi = C.POINTER(C.POINTER(C.c_int))
@@ -85,6 +85,11 @@ SIGNATURES = {
     "gbsym_parsy_H2LeveledBlockedLTsolve": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _vp, _vp, _int, _vp, _vp, _int]),
     "gbsym_parsy_H2LeveledBlockedLsolve_mrhs": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _int, _vp, _vp, _int, _vp, _vp, _int, _int]),
     "gbsym_parsy_H2LeveledBlockedLTsolve_mrhs": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _int, _vp, _vp, _int, _vp, _vp, _int, _int]),
+    "gbsym_parsy_solve_phase_ll_blocked": (None, [_sz, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _int]),
+    "gbsym_parsy_solve_phase_ll_blocked_nrhs": (None, [_sz, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _int, _int]),
+    "gbsym_parsy_solve_phase_ll_blocked_parallel": (None, [_sz, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _int, _int, _vp, _vp, _int, _vp, _vp, _int]),
+    "gbsym_parsy_solve_phase_ll_blocked_parallel_nrhs": (None, [_sz, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _int, _int, _vp, _vp, _int, _vp, _vp, _int, _int]),
+    "gbsym_parsy_solve_phase_ldl": (None, [_sz, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _int]),
     "gbsym_sn_create": (_int, [_vp, _int, _vp, _vp, _vp, _vp, _vp, _int, _vp]),
     "gbsym_sn_destroy": (_int, [_vp]),
     "gbsym_sn_levels": (_int, [_vp, _vp, _vp]),

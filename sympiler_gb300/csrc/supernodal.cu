@@ -892,6 +892,47 @@ void sn_dropin(int n, const size_t *Lp, const int *Li, const double *Lx, const s
   GB_CUDA(cudaStreamSynchronize(s));
 }
 
+// x[i] /= d[i] for every right-hand side (IEEE division, as
+// parsy::scale_vec_vec, solve_phase.cpp:15-21).
+__global__ void k_scale_div(double *__restrict__ x, const double *__restrict__ d, int n, int k) {
+  const size_t m = (size_t)n * k;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < m; i += (size_t)gridDim.x * blockDim.x)
+    x[i] = __ddiv_rn(x[i], d[i % n]);
+}
+
+// The LL^T (and LDL^T) solve phases: one plan, the forward solve, the
+// diagonal scaling when d is given, the transposed solve.  A schedule is
+// validated for both directions (the transposed solve walks it backward,
+// as parsy::solve_phase_ll_blocked_parallel passes it to both,
+// solve_phase.cpp:58-75).
+void sn_dropin_phase(int n, const size_t *Lp, const int *Li, const double *Lx, const size_t *Li_ptr,
+                     const int *sup2col, int supNo, const double *d, double *x, int k, int levels,
+                     const int *level_ptr, const int *par_ptr, const int *partition) {
+  GB_CHECK(k >= 0, GBSYM_ERR_SIZE);
+  if (n == 0 || k == 0) return;
+  GB_CHECK(x, GBSYM_ERR_NULL_ARG);
+  cudaStream_t s = thread_stream();
+  std::unique_ptr<gbsym_sn_s> t(sn_build(n, Lp, Li, Lx, Li_ptr, sup2col, supNo, s));
+  if (par_ptr) {
+    sn_validate_lbc(t.get(), Li_ptr, Li, sup2col, levels, level_ptr, par_ptr, partition, false);
+    sn_validate_lbc(t.get(), Li_ptr, Li, sup2col, levels, level_ptr, par_ptr, partition, true);
+  }
+  DBuf<double> dx, dd;
+  upload(dx, x, (size_t)n * k, false, s);
+  sn_solve(t.get(), dx.p, k, false, s);
+  if (d) {
+    upload(dd, d, (size_t)n, false, s);
+    const int grid = (int)std::min<size_t>(div_up((size_t)n * k, (size_t)256), (size_t)num_sms() * 8);
+    k_scale_div<<<std::max(1, grid), 256, 0, s>>>(dx.p, dd.p, n, k);
+    check_launch();
+  }
+  sn_solve(t.get(), dx.p, k, true, s);
+  const int code = sn_read_error(t.get(), s);
+  if (code) throw Err{code};
+  GB_CUDA(cudaMemcpyAsync(x, dx.p, (size_t)n * k * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+}
+
 // A plain level set over supernodes, validated as the one-part-per-node LBC
 // schedule it is.
 void sn_dropin_levels(int n, const size_t *Lp, const int *Li, const double *Lx, const size_t *Li_ptr,
@@ -1047,6 +1088,73 @@ int gbsym_parsy_H2LeveledBlockedLTsolve_mrhs(GBSYM_SN_ARGS, int m_rhs, int level
               partition);
   }));
   return status_to_int();
+}
+
+#define GBSYM_PHASE_ARGS                                                                                  \
+  int *col2sup, int *sup2col, size_t *newCol, int *newRow, double *newVal, size_t *rowP, size_t nBlocks, int nnz
+
+static int phase_n(size_t n, size_t nBlocks) {
+  GB_CHECK(n <= (size_t)INT_MAX && nBlocks <= (size_t)INT_MAX, GBSYM_ERR_SIZE);
+  return (int)n;
+}
+
+void gbsym_parsy_solve_phase_ll_blocked(size_t n, double *x, GBSYM_PHASE_ARGS) {
+  (void)col2sup;
+  (void)nnz;
+  set_last_error(guarded([&] {
+    sn_dropin_phase(phase_n(n, nBlocks), newCol, newRow, newVal, rowP, sup2col, (int)nBlocks, nullptr, x, 1, 0,
+                    nullptr, nullptr, nullptr);
+  }));
+}
+
+void gbsym_parsy_solve_phase_ll_blocked_nrhs(size_t n, double *x, int n_rhs, GBSYM_PHASE_ARGS, int max_col) {
+  (void)col2sup;
+  (void)nnz;
+  (void)max_col;
+  set_last_error(guarded([&] {
+    sn_dropin_phase(phase_n(n, nBlocks), newCol, newRow, newVal, rowP, sup2col, (int)nBlocks, nullptr, x, n_rhs, 0,
+                    nullptr, nullptr, nullptr);
+  }));
+}
+
+void gbsym_parsy_solve_phase_ll_blocked_parallel(size_t n, double *x, GBSYM_PHASE_ARGS, int levels, int *levelPtr,
+                                                 int *levelSet, int parts, int *parPtr, int *partition, int chunk) {
+  (void)col2sup;
+  (void)nnz;
+  (void)levelSet;
+  (void)parts;
+  (void)chunk;
+  set_last_error(guarded([&] {
+    GB_CHECK(n == 0 || (levelPtr && parPtr && partition), GBSYM_ERR_NULL_ARG);
+    sn_dropin_phase(phase_n(n, nBlocks), newCol, newRow, newVal, rowP, sup2col, (int)nBlocks, nullptr, x, 1, levels,
+                    levelPtr, n ? parPtr : nullptr, partition);
+  }));
+}
+
+void gbsym_parsy_solve_phase_ll_blocked_parallel_nrhs(size_t n, double *x, int n_rhs, GBSYM_PHASE_ARGS, int levels,
+                                                      int *levelPtr, int *levelSet, int parts, int *parPtr,
+                                                      int *partition, int chunk, int max_col) {
+  (void)col2sup;
+  (void)nnz;
+  (void)levelSet;
+  (void)parts;
+  (void)chunk;
+  (void)max_col;
+  set_last_error(guarded([&] {
+    GB_CHECK(n == 0 || (levelPtr && parPtr && partition), GBSYM_ERR_NULL_ARG);
+    sn_dropin_phase(phase_n(n, nBlocks), newCol, newRow, newVal, rowP, sup2col, (int)nBlocks, nullptr, x, n_rhs,
+                    levels, levelPtr, n ? parPtr : nullptr, partition);
+  }));
+}
+
+void gbsym_parsy_solve_phase_ldl(size_t n, double *d_val, double *x, GBSYM_PHASE_ARGS) {
+  (void)col2sup;
+  (void)nnz;
+  set_last_error(guarded([&] {
+    GB_CHECK(n == 0 || d_val, GBSYM_ERR_NULL_ARG);
+    sn_dropin_phase(phase_n(n, nBlocks), newCol, newRow, newVal, rowP, sup2col, (int)nBlocks, d_val, x, 1, 0,
+                    nullptr, nullptr, nullptr);
+  }));
 }
 
 }  // extern "C"

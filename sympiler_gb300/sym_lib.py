@@ -248,6 +248,55 @@ class parsy:  # noqa: N801 -- mirrors the reference's nested namespace
         return fn(*parsy._sn(S), _p(X), int(n_rhs), int(levels), _p(lp), None, int(parts), _p(pp), _p(pa),
                   int(chunk), int(max_col))
 
+    # solve phases: (n, x, ..., col2sup, sup2col, Lp, Li, Lx, Li_ptr, nsup, nnz)
+    @staticmethod
+    def _phase(S):
+        return (_p(_arr(S.col2sup, _I32, "col2sup")), _p(_arr(S.sup2col, _I32, "sup2col")),
+                _p(_arr(S.Lp, np.uint64, "Lp")), _p(_arr(S.Li, _I32, "Li")), _p(_arr(S.Lx, _F64, "Lx")),
+                _p(_arr(S.Li_ptr, np.uint64, "Li_ptr")), int(S.nsup), 0)
+
+    @staticmethod
+    def solve_phase_ll_blocked(S, x):
+        """solve_phase.cpp:39-46 -- L then L^T, in place (raises on error)."""
+        x = _arr(x, _F64, "x", True)
+        lib().gbsym_parsy_solve_phase_ll_blocked(int(S.n), _p(x), *parsy._phase(S))
+        _raise_last("solve_phase_ll_blocked")
+
+    @staticmethod
+    def solve_phase_ll_blocked_nrhs(S, X, n_rhs, max_col=-1):
+        X = _arr(X, _F64, "X", True)
+        a = parsy._phase(S)
+        lib().gbsym_parsy_solve_phase_ll_blocked_nrhs(int(S.n), _p(X), int(n_rhs), *a, int(max_col))
+        _raise_last("solve_phase_ll_blocked_nrhs")
+
+    @staticmethod
+    def solve_phase_ll_blocked_parallel(S, x, levels, levelPtr, parts, parPtr, partition, chunk=1):  # noqa: N803
+        x = _arr(x, _F64, "x", True)
+        lp, pp, pa = (_arr(levelPtr, _I32, "levelPtr"), _arr(parPtr, _I32, "parPtr"),
+                      _arr(partition, _I32, "partition"))
+        lib().gbsym_parsy_solve_phase_ll_blocked_parallel(int(S.n), _p(x), *parsy._phase(S), int(levels), _p(lp),
+                                                          None, int(parts), _p(pp), _p(pa), int(chunk))
+        _raise_last("solve_phase_ll_blocked_parallel")
+
+    @staticmethod
+    def solve_phase_ll_blocked_parallel_nrhs(S, X, n_rhs, levels, levelPtr, parts, parPtr, partition,  # noqa: N803
+                                             chunk=1, max_col=-1):
+        X = _arr(X, _F64, "X", True)
+        lp, pp, pa = (_arr(levelPtr, _I32, "levelPtr"), _arr(parPtr, _I32, "parPtr"),
+                      _arr(partition, _I32, "partition"))
+        lib().gbsym_parsy_solve_phase_ll_blocked_parallel_nrhs(int(S.n), _p(X), int(n_rhs), *parsy._phase(S),
+                                                               int(levels), _p(lp), None, int(parts), _p(pp),
+                                                               _p(pa), int(chunk), int(max_col))
+        _raise_last("solve_phase_ll_blocked_parallel_nrhs")
+
+    @staticmethod
+    def solve_phase_ldl(S, d_val, x):
+        """solve_phase.cpp:96-112 -- L, x /= d, L^T, in place."""
+        x = _arr(x, _F64, "x", True)
+        d = _arr(d_val, _F64, "d_val")
+        lib().gbsym_parsy_solve_phase_ldl(int(S.n), _p(d), _p(x), *parsy._phase(S))
+        _raise_last("solve_phase_ldl")
+
     @staticmethod
     def lus_cr(n, nz_num, ia, ja, l, ua, r, z):
         """sparse_blas/parsy/gmres/mgmres.cpp:598-689 -- z = (LU)^{-1} r."""

@@ -74,6 +74,8 @@ int main(int argc, char **argv) {
     size_t zp[2] = {0, 1};
     sym_lib::parsy::blockedLsolve(n, zp, i, v, 1, zp, i, p, 1, x);
     sym_lib::parsy::H2LeveledBlockedLTsolve(n, zp, i, v, 1, zp, i, p, 1, x, 1, p, i, 1, p, i, 1);
+    sym_lib::parsy::solve_phase_ll_blocked(1, x, i, p, zp, i, v, zp, 1, 1);
+    sym_lib::parsy::solve_phase_ldl(1, v, x, i, p, zp, i, v, zp, 1, 1);
     sym_lib::build_levelSet_CSC(1, p, i, lp, ls);
     delete[] lp; delete[] ls;
   }

@@ -254,6 +254,46 @@ def test_gpu_supernodal_degenerate_shapes(gpu, orc):
 
 
 @pytest.mark.gpu
+def test_gpu_solve_phases(gpu, orc):
+    """parsy's LL^T solve phases (L then L^T, serial, multi-RHS and
+    LBC-scheduled) and the LDL^T phase with a diagonal D, against the
+    restatement run in the same order."""
+    from sympiler_gb300 import sym_lib
+    S = mg.nd_supernodal(14, 12, 10, leaf=27, rng=np.random.default_rng(12))
+    rng = np.random.default_rng(13)
+    b = rng.standard_normal(S.n)
+    want = b.copy()
+    orc.blocked_lsolve(S, want)
+    orc.blocked_ltsolve(S, want)
+    x = b.copy()
+    sym_lib.parsy.solve_phase_ll_blocked(S, x)
+    assert np.array_equal(x, want)
+    nl, lp, ls = _sn_levels(S)
+    pp = np.arange(S.nsup + 1, dtype=np.int32)
+    x = b.copy()
+    sym_lib.parsy.solve_phase_ll_blocked_parallel(S, x, nl, lp, S.nsup, pp, ls)
+    assert np.array_equal(x, want)
+    X = rng.standard_normal((3, S.n))
+    W = X.copy()
+    orc.blocked_lsolve(S, W)
+    orc.blocked_ltsolve(S, W)
+    Y = X.copy()
+    sym_lib.parsy.solve_phase_ll_blocked_nrhs(S, Y, 3)
+    assert np.array_equal(Y, W)
+    Y = X.copy()
+    sym_lib.parsy.solve_phase_ll_blocked_parallel_nrhs(S, Y, 3, nl, lp, S.nsup, pp, ls)
+    assert np.array_equal(Y, W)
+    d = rng.uniform(0.5, 2.0, S.n)
+    want = b.copy()
+    orc.blocked_lsolve(S, want)
+    want = want / d
+    orc.blocked_ltsolve(S, want)
+    x = b.copy()
+    sym_lib.parsy.solve_phase_ldl(S, d, x)
+    assert np.array_equal(x, want)
+
+
+@pytest.mark.gpu
 def test_gpu_supernodal_rejects_malformed_storage(gpu):
     from sympiler_gb300 import sym_lib
     from sympiler_gb300._lib import ERR_BAD_MATRIX as GBSYM_ERR_BAD_MATRIX, lib
