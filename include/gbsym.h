@@ -264,6 +264,16 @@ int gbsym_parsy_H2LeveledBlockedLTsolve_mrhs(
     int *levelPtr, int *levelSet, int parts, int *parPtr, int *partition,
     int chunk, int max_col);
 
+/* The simplicial (CSC) solve phases: parsy::lsolve, then for LDL^T
+ * x[i] /= d_val[i], then parsy::ltsolve, on the GPU; x in place; void (the
+ * status is in gbsym_last_error()).  Replace parsy::solve_phase_simplicial_ll
+ * and _ldl (sparse_blas/parsy/linear_solver/solve_phase.cpp:23-37). */
+void gbsym_parsy_solve_phase_simplicial_ll(int n, int *Lp, int *Li, double *Lx,
+                                           double *x);
+void gbsym_parsy_solve_phase_simplicial_ldl(int n, int *Lp, int *Li,
+                                            double *Lx, double *d_val,
+                                            double *x);
+
 /* The supernodal LL^T solve phases: the forward solve, then the transposed
  * one, on one resident plan; x (n x n_rhs, column-major) in place.  void,
  * as in the reference: the status is in gbsym_last_error().  The

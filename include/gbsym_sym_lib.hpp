@@ -228,6 +228,13 @@ inline int H2LeveledBlockedLTsolve_mrhs(int n, size_t *Lp, int *Li, double *Lx, 
                                                   levels, levelPtr, levelSet, parts, parPtr, partition, chunk,
                                                   max_col);
 }
+// linear_solver/solve_phase.h:21-29
+inline void solve_phase_simplicial_ll(int n, int *Lp, int *Li, double *Lx, double *x) {
+  gbsym_parsy_solve_phase_simplicial_ll(n, Lp, Li, Lx, x);
+}
+inline void solve_phase_simplicial_ldl(int n, int *Lp, int *Li, double *Lx, double *d_val, double *x) {
+  gbsym_parsy_solve_phase_simplicial_ldl(n, Lp, Li, Lx, d_val, x);
+}
 // linear_solver/solve_phase.h:35-62
 inline void solve_phase_ll_blocked(size_t n, double *x, int *col2sup, int *sup2col, size_t *newCol, int *newRow,
                                    double *newVal, size_t *rowP, size_t nBlocks, int nnz) {

@@ -85,6 +85,8 @@ SIGNATURES = {
     "gbsym_parsy_H2LeveledBlockedLTsolve": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _vp, _vp, _int, _vp, _vp, _int]),
     "gbsym_parsy_H2LeveledBlockedLsolve_mrhs": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _int, _vp, _vp, _int, _vp, _vp, _int, _int]),
     "gbsym_parsy_H2LeveledBlockedLTsolve_mrhs": (_int, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp, _int, _vp, _int, _int, _vp, _vp, _int, _vp, _vp, _int, _int]),
+    "gbsym_parsy_solve_phase_simplicial_ll": (None, [_int, _vp, _vp, _vp, _vp]),
+    "gbsym_parsy_solve_phase_simplicial_ldl": (None, [_int, _vp, _vp, _vp, _vp, _vp]),
     "gbsym_parsy_solve_phase_ll_blocked": (None, [_sz, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _int]),
     "gbsym_parsy_solve_phase_ll_blocked_nrhs": (None, [_sz, _vp, _int, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _int, _int]),
     "gbsym_parsy_solve_phase_ll_blocked_parallel": (None, [_sz, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _int, _int, _vp, _vp, _int, _vp, _vp, _int]),

@@ -162,6 +162,47 @@ static void csc_dropin(int n, const int *Lp, const int *Li, const double *Lx, do
   GB_CUDA(cudaStreamSynchronize(s));
 }
 
+__global__ void k_div_by_vec(double *__restrict__ x, const double *__restrict__ d, int n) {
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+    x[t] = __ddiv_rn(x[t], d[t]);
+}
+
+// parsy's simplicial solve phases (solve_phase.cpp:23-37): lsolve on the
+// CSC of L (the column-push order, reproduced by the pull form), x /= d
+// for LDL^T (IEEE division, as scale_vec_vec), then ltsolve on the same
+// CSC read as an upper CSR with the diagonal first.
+static void simplicial_phase(int n, const int *Lp, const int *Li, const double *Lx, const double *d, double *x) {
+  GB_CHECK(n >= 0, GBSYM_ERR_SIZE);
+  if (n == 0) return;
+  GB_CHECK(Lp && Li && Lx && x, GBSYM_ERR_NULL_ARG);
+  cudaStream_t s = thread_stream();
+  DevCsr L;
+  csc_lower_to_csr(n, Lp, Li, Lx, L, s);
+  const int nnz = Lp[n];
+  DBuf<int> cp, ci;
+  DBuf<double> cx, dx, dd;
+  upload(cp, Lp, n + 1, false, s);
+  upload(ci, Li, nnz, false, s);
+  upload(cx, Lx, nnz, false, s);
+  std::unique_ptr<gbsym_tri_s> lo(tri_build(n, L.p.p, L.i.p, L.x.p, nullptr, GBSYM_LOWER_DIAG_LAST, GBSYM_F64,
+                                            nullptr, nullptr, 0, s));
+  std::unique_ptr<gbsym_tri_s> up(tri_build(n, cp.p, ci.p, cx.p, nullptr, GBSYM_UPPER_DIAG_FIRST, GBSYM_F64,
+                                            nullptr, nullptr, 0, s));
+  upload(dx, x, n, false, s);
+  tri_solve_rowmajor(lo.get(), dx.p, nullptr, 1, GBSYM_F64, s);
+  if (d) {
+    upload(dd, d, n, false, s);
+    k_div_by_vec<<<std::max(1, std::min(div_up(n, 256), num_sms() * 8)), 256, 0, s>>>(dx.p, dd.p, n);
+    check_launch();
+  }
+  tri_solve_rowmajor(up.get(), dx.p, nullptr, 1, GBSYM_F64, s);
+  int code = tri_read_error(lo.get(), s);
+  if (!code) code = tri_read_error(up.get(), s);
+  if (code) throw Err{code};
+  GB_CUDA(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+}
+
 static int max_col_plus_one(int n, const int *Ap, const int *Ai) {
   int m = n;
   for (int e = Ap[0]; e < Ap[n]; ++e) m = std::max(m, Ai[e] + 1);
@@ -364,6 +405,17 @@ int gbsym_parsy_lsolve(int n, int *Lp, int *Li, double *Lx, double *x) {
 
 int gbsym_parsy_ltsolve(int n, int *Lp, int *Li, double *Lx, double *x) {
   return gbsym_ltsolve(n, Lp, Li, Lx, x);
+}
+
+void gbsym_parsy_solve_phase_simplicial_ll(int n, int *Lp, int *Li, double *Lx, double *x) {
+  record([&] { simplicial_phase(n, Lp, Li, Lx, nullptr, x); });
+}
+
+void gbsym_parsy_solve_phase_simplicial_ldl(int n, int *Lp, int *Li, double *Lx, double *d_val, double *x) {
+  record([&] {
+    GB_CHECK(n <= 0 || d_val, GBSYM_ERR_NULL_ARG);
+    simplicial_phase(n, Lp, Li, Lx, d_val, x);
+  });
 }
 
 int gbsym_parsy_lsolvePar(int n, int *Lp, int *Li, double *Lx, double *x, int levels,

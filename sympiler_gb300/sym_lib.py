@@ -248,6 +248,22 @@ class parsy:  # noqa: N801 -- mirrors the reference's nested namespace
         return fn(*parsy._sn(S), _p(X), int(n_rhs), int(levels), _p(lp), None, int(parts), _p(pp), _p(pa),
                   int(chunk), int(max_col))
 
+    @staticmethod
+    def solve_phase_simplicial_ll(n, Lp, Li, Lx, x):  # noqa: N803
+        """solve_phase.cpp:23-28 -- lsolve then ltsolve on the CSC of L."""
+        Lp, Li, Lx = _arr(Lp, _I32, "Lp"), _arr(Li, _I32, "Li"), _arr(Lx, _F64, "Lx")
+        x = _arr(x, _F64, "x", True)
+        lib().gbsym_parsy_solve_phase_simplicial_ll(int(n), _p(Lp), _p(Li), _p(Lx), _p(x))
+        _raise_last("solve_phase_simplicial_ll")
+
+    @staticmethod
+    def solve_phase_simplicial_ldl(n, Lp, Li, Lx, d_val, x):  # noqa: N803
+        """solve_phase.cpp:30-37 -- lsolve, x /= d, ltsolve."""
+        Lp, Li, Lx = _arr(Lp, _I32, "Lp"), _arr(Li, _I32, "Li"), _arr(Lx, _F64, "Lx")
+        d, x = _arr(d_val, _F64, "d_val"), _arr(x, _F64, "x", True)
+        lib().gbsym_parsy_solve_phase_simplicial_ldl(int(n), _p(Lp), _p(Li), _p(Lx), _p(d), _p(x))
+        _raise_last("solve_phase_simplicial_ldl")
+
     # solve phases: (n, x, ..., col2sup, sup2col, Lp, Li, Lx, Li_ptr, nsup, nnz)
     @staticmethod
     def _phase(S):

@@ -76,6 +76,8 @@ int main(int argc, char **argv) {
     sym_lib::parsy::H2LeveledBlockedLTsolve(n, zp, i, v, 1, zp, i, p, 1, x, 1, p, i, 1, p, i, 1);
     sym_lib::parsy::solve_phase_ll_blocked(1, x, i, p, zp, i, v, zp, 1, 1);
     sym_lib::parsy::solve_phase_ldl(1, v, x, i, p, zp, i, v, zp, 1, 1);
+    sym_lib::parsy::solve_phase_simplicial_ll(n, p, i, v, x);
+    sym_lib::parsy::solve_phase_simplicial_ldl(n, p, i, v, v, x);
     sym_lib::build_levelSet_CSC(1, p, i, lp, ls);
     delete[] lp; delete[] ls;
   }

@@ -294,6 +294,33 @@ def test_gpu_solve_phases(gpu, orc):
 
 
 @pytest.mark.gpu
+def test_gpu_simplicial_solve_phases(gpu, orc):
+    """parsy's simplicial solve phases on the CSC of an IC0 factor (the
+    upper CSR of the factored triangle): lsolve, (x /= d), ltsolve, each
+    the oracle's bits."""
+    from sympiler_gb300 import sym_lib
+    A = mg.lap2d(40)
+    U = mg.triu(A)
+    f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+    assert ok
+    Lp, Li, Lx = U.p, U.i, f  # CSC of L, diagonal first in each column
+    b = np.random.default_rng(14).standard_normal(U.n)
+    d = np.random.default_rng(15).uniform(0.5, 2.0, U.n)
+    for dv in (None, d):
+        want = b.copy()
+        orc.sptrsv_csc(U.n, Lp, Li, Lx, want)
+        if dv is not None:
+            want = want / dv
+        orc.ltsolve(U.n, Lp, Li, Lx, want)
+        x = b.copy()
+        if dv is None:
+            sym_lib.parsy.solve_phase_simplicial_ll(U.n, Lp, Li, Lx, x)
+        else:
+            sym_lib.parsy.solve_phase_simplicial_ldl(U.n, Lp, Li, Lx, dv, x)
+        assert np.array_equal(x, want)
+
+
+@pytest.mark.gpu
 def test_gpu_supernodal_rejects_malformed_storage(gpu):
     from sympiler_gb300 import sym_lib
     from sympiler_gb300._lib import ERR_BAD_MATRIX as GBSYM_ERR_BAD_MATRIX, lib
