@@ -83,7 +83,7 @@ struct SnQueue {
 }  // namespace gbsym
 
 struct gbsym_sn_s {
-  int n = 0, nsup = 0, nlev = 0, nblev = 0, max_w = 0;
+  int n = 0, nsup = 0, nlev = 0, nblev = 0;
   int grid = 0;              // blocks of the persistent launch
   int groups = 0;            // right-hand-side groups the counters are laid out for
   unsigned long long ef = 0, et = 0;  // solves since the counters were cleared
@@ -465,17 +465,17 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
         for (int p = V.pull_ptr[c0 + q]; p < p1; p += 8) {
           size_t ci[8];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) ci[u] = p + u < p1 ? (size_t)__ldg(V.pull_idx + p + u) : 0;
+          for (int b = 0; b < 8; ++b) ci[b] = p + b < p1 ? (size_t)__ldg(V.pull_idx + p + b) : 0;
 #pragma unroll
           for (int j = 0; j < KR; ++j)
             if (j < kr) {
               const double *cb = V.contrib + (size_t)(j0 + j) * V.ncontrib;
               double cv[8];
 #pragma unroll
-              for (int u = 0; u < 8; ++u) cv[u] = p + u < p1 ? __ldcg(cb + ci[u]) : 0.0;
+              for (int b = 0; b < 8; ++b) cv[b] = p + b < p1 ? __ldcg(cb + ci[b]) : 0.0;
 #pragma unroll
-              for (int u = 0; u < 8; ++u)
-                if (p + u < p1) v[j] = xsub(v[j], cv[u]);
+              for (int b = 0; b < 8; ++b)
+                if (p + b < p1) v[j] = xsub(v[j], cv[b]);
             }
         }
       }
@@ -671,7 +671,6 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
     for (size_t k = r0 + (z - a); k < r1; ++k)  // off-block rows below the supernode, ascending
       GB_CHECK(Li[k] >= z && Li[k] < n && (k == r0 + (z - a) || Li[k] > Li[k - 1]), GBSYM_ERR_BAD_MATRIX);
     nvals = std::max(nvals, (size_t)Lp[a] + (r1 - r0) * (size_t)(z - a));
-    t->max_w = std::max(t->max_w, z - a);
   }
   c0[nsup] = n;
   GB_CHECK(ncontrib < INT_MAX, GBSYM_ERR_UNSUPPORTED);
