@@ -324,6 +324,13 @@ int gbsym_sn_destroy(gbsym_sn t);
 int gbsym_sn_levels(gbsym_sn t, int *forward_levels, int *transposed_levels);
 int gbsym_sn_solve(gbsym_sn t, double *x, int k, int transposed, void *stream);
 int gbsym_sn_check(gbsym_sn t, void *stream);
+/* Bounded-wait self-test: one forward solve on scratch data whose counter
+ * targets are one epoch ahead, so its waits on contributions cannot
+ * complete and give up after limit_cycles SM cycles.  Returns the error
+ * word the launch left (GBSYM_ERR_TIMEOUT where some supernode receives
+ * contributions), then clears the plan's counters; later solves are
+ * unaffected.  No fault, no hang: every wait is bounded. */
+int gbsym_sn_selftest_timeout(gbsym_sn t, long long limit_cycles, void *stream);
 
 /* ======================================================================== */
 /* Plans (device-resident).                                                 */

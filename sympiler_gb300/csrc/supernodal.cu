@@ -133,6 +133,7 @@ struct SnView {
   double *x, *contrib, *y;
   long long ncontrib;
   unsigned long long epoch, base[2];
+  long long wait_cycles;  // bounded waits give up after this many SM cycles
   int *err;
 };
 
@@ -217,14 +218,14 @@ __device__ __forceinline__ double quotient(double a, double b, double y, const D
 // about two seconds, recording GBSYM_ERR_TIMEOUT, or at once when another
 // wait has; the task then runs on, so every counter still reaches its
 // target and the launch ends.
-__device__ bool sn_wait(const unsigned long long *f, unsigned long long want, int *err) {
+__device__ bool sn_wait(const unsigned long long *f, unsigned long long want, int *err, long long limit) {
   if (__all_sync(kFull, ld_acq64(f) >= want)) return true;
   const long long t0 = __shfl_sync(kFull, clock64(), 0);
   for (;;) {
     __nanosleep(40);
     if (__all_sync(kFull, ld_acq64(f) >= want)) return true;
     if (__any_sync(kFull, ld_relaxed(err) != 0)) return false;
-    if (__shfl_sync(kFull, clock64() - t0 > kSnWaitCycles, 0)) {
+    if (__shfl_sync(kFull, clock64() - t0 > limit, 0)) {
       if ((threadIdx.x & 31) == 0) atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
       return false;
     }
@@ -279,7 +280,8 @@ struct Runs {
 template <int KR, bool TR>
 __device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool act, const double *__restrict__ E,
                                             size_t estride, const int *__restrict__ idx, const double *xb,
-                                            size_t xstride, int kr, double (&acc)[KR], int *err, bool &failed) {
+                                            size_t xstride, int kr, double (&acc)[KR], int *err, long long limit,
+                                            bool &failed) {
   const Runs R(len);
 #pragma unroll
   for (int j = 0; j < KR; ++j) acc[j] = 0.0;
@@ -301,7 +303,7 @@ __device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool
           __nanosleep(ns);
           ns = min(2 * ns, 1024);
           if (__any_sync(kFull, ld_relaxed(err) != 0)) failed = true;
-          if (__shfl_sync(kFull, clock64() - t0 > kSnWaitCycles, 0)) {
+          if (__shfl_sync(kFull, clock64() - t0 > limit, 0)) {
             if (lane_zero()) atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
             failed = true;
           }
@@ -342,7 +344,7 @@ __device__ __forceinline__ void grouped_sum(int len, int H, int rho, int h, bool
           if (t0 == 0) t0 = __shfl_sync(kFull, clock64(), 0);
           __nanosleep(100);
           if (__any_sync(kFull, ld_relaxed(err) != 0)) failed = true;
-          if (__shfl_sync(kFull, clock64() - t0 > kSnWaitCycles, 0)) {
+          if (__shfl_sync(kFull, clock64() - t0 > limit, 0)) {
             if ((threadIdx.x & 31) == 0) atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
             failed = true;
           }
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
         d = __ldg(M + (size_t)q * ld + q);
         y = __drcp_rn(d);
       }
-      sn_wait(V.in + fi, V.epoch * (unsigned long long)(fwd ? V.need_in[t] : V.n_ot[t]), V.err);
+      sn_wait(V.in + fi, V.epoch * (unsigned long long)(fwd ? V.need_in[t] : V.n_ot[t]), V.err, V.wait_cycles);
       double v[KR];
 #pragma unroll
       for (int j = 0; j < KR; ++j) v[j] = (act && j < kr) ? __ldcg(xg + (size_t)j * V.n + c0 + q) : 0.0;
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
             if (t0 == 0) t0 = __shfl_sync(kFull, clock64(), 0);
             __nanosleep(20);
             if (__any_sync(kFull, ld_relaxed(V.err) != 0)) failed = true;
-            if (__shfl_sync(kFull, clock64() - t0 > kSnWaitCycles, 0)) {
+            if (__shfl_sync(kFull, clock64() - t0 > V.wait_cycles, 0)) {
               if (lane == 0) atomicCAS(V.err, 0, GBSYM_ERR_TIMEOUT);
               failed = true;
             }
@@ -579,7 +581,7 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
         const int o = T.a + rho;
         const bool act = o < ld - w;
         grouped_sum<KR, false>(w, H, rho, h, act, M + w + o, ld, nullptr, V.y + (size_t)j0 * V.n + c0, V.n, kr, acc,
-                               V.err, failed);
+                               V.err, V.wait_cycles, failed);
         if (act && h == 0) {
 #pragma unroll
           for (int j = 0; j < KR; ++j)
@@ -595,7 +597,7 @@ __global__ void __launch_bounds__(kSnWarps * 32) k_sn(SnView V) {
         const int col = T.a + rho;
         const bool act = col < w;
         grouped_sum<KR, true>(ld - w, H, rho, h, act, M + (size_t)col * ld + w, 1, V.rows + V.rb[t] + w,
-                              V.y + (size_t)j0 * V.n, V.n, kr, acc, V.err, failed);
+                              V.y + (size_t)j0 * V.n, V.n, kr, acc, V.err, V.wait_cycles, failed);
         if (act && h == 0) {
 #pragma unroll
           for (int j = 0; j < KR; ++j)
@@ -772,7 +774,10 @@ gbsym_sn_s *sn_build(int n, const size_t *Lp, const int *Li, const double *Lx, c
   return t.release();
 }
 
-void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) {
+// skew > 0 sets every counter target that many epochs ahead, so waits on
+// counters cannot complete (the bounded-wait self-test).
+void sn_launch(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s, unsigned long long skew,
+               long long wait_cycles) {
   if (t->n == 0 || k == 0) return;
   const int G = (k + kSnRhs - 1) / kSnRhs;
   const size_t per = (size_t)t->nsup * G;
@@ -826,9 +831,14 @@ void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) 
     Q.ctr += (unsigned long long)Q.ntask * G + (unsigned long long)grid * (role == 0 ? 1 : kSnWarps - 1);
   }
   V.in = f + 4 + (transposed ? per : 0);
-  V.epoch = transposed ? ++t->et : ++t->ef;
+  V.epoch = (transposed ? ++t->et : ++t->ef) + skew;
+  V.wait_cycles = wait_cycles;
   k_sn<kSnRhs><<<grid, kSnWarps * 32, 0, s>>>(V);
   check_launch();
+}
+
+void sn_solve(gbsym_sn_s *t, double *x, int k, bool transposed, cudaStream_t s) {
+  sn_launch(t, x, k, transposed, s, 0, kSnWaitCycles);
 }
 
 int sn_read_error(gbsym_sn_s *t, cudaStream_t s) {
@@ -976,6 +986,25 @@ int gbsym_sn_solve(gbsym_sn t, double *x, int k, int transposed, void *stream) {
   if (!t || (!x && t->n && k)) return GBSYM_ERR_NULL_ARG;
   if (k < 0) return GBSYM_ERR_SIZE;
   return guarded([&] { sn_solve(t, x, k, transposed != 0, (cudaStream_t)stream); });
+}
+
+int gbsym_sn_selftest_timeout(gbsym_sn t, long long limit_cycles, void *stream) {
+  if (!t) return GBSYM_ERR_NULL_ARG;
+  if (t->n == 0 || limit_cycles <= 0) return GBSYM_ERR_SIZE;
+  int code = 0;
+  const int st = guarded([&] {
+    cudaStream_t s = (cudaStream_t)stream;
+    DBuf<double> x((size_t)t->n);
+    GB_CUDA(cudaMemsetAsync(x.p, 0, (size_t)t->n * sizeof(double), s));
+    sn_launch(t, x.p, 1, false, s, 1, limit_cycles);
+    code = sn_read_error(t, s);
+    // the counters no longer match any epoch: start them afresh
+    if (t->flags.p) GB_CUDA(cudaMemsetAsync(t->flags.p, 0, t->flags.n * sizeof(unsigned long long), s));
+    t->ef = t->et = 0;
+    for (auto &qq : t->q) qq.ctr = 0;
+    GB_CUDA(cudaStreamSynchronize(s));
+  });
+  return st != GBSYM_OK ? st : code;
 }
 
 int gbsym_sn_check(gbsym_sn t, void *stream) {

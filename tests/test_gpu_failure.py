@@ -28,6 +28,25 @@ def test_bounded_wait_times_out_and_context_survives(gpu, orc):
     assert np.array_equal(x.cpu().numpy(), ref)
 
 
+def test_supernodal_waits_time_out_and_plan_recovers(gpu, orc):
+    """The supernodal task graph's bounded waits: a solve whose counter
+    targets cannot be reached gives up after the limit (about 50 ms here),
+    reports GBSYM_ERR_TIMEOUT, and the same plan then solves bit-exactly."""
+    from sympiler_gb300._lib import ERR_TIMEOUT, lib
+    from sympiler_gb300.plans import SupernodalPlan
+    S = mg.nd_supernodal(12, 10, 9, leaf=16, rng=np.random.default_rng(3))
+    P = SupernodalPlan(S)
+    assert lib().gbsym_sn_selftest_timeout(P._h, 100_000_000, None) == ERR_TIMEOUT
+    b = np.random.default_rng(4).standard_normal(S.n)
+    for transposed in (False, True, False):
+        want = b.copy()
+        (orc.blocked_ltsolve if transposed else orc.blocked_lsolve)(S, want)
+        x = torch.from_numpy(b.copy()).cuda()
+        P.solve(x, transposed=transposed)
+        P.check()
+        assert np.array_equal(x.cpu().numpy(), want)
+
+
 def test_zero_pivot_reported_not_trapped(gpu):
     from sympiler_gb300 import sym_lib
     from sympiler_gb300._lib import ERR_PIVOT, GbsymError
