@@ -213,14 +213,44 @@ __global__ void k_scale(long long n, double alpha, const double *__restrict__ u,
     v[i] = alpha * u[i];
 }
 
-// One fused modified Gram-Schmidt pass over v:
+// The sum of m block partials, as k_reduce_final forms it (same threads,
+// same order), by the block that arrives last: every block publishes its
+// partials, then takes a ticket; the block holding the last ticket reads
+// them back through L2, stores the sums and resets the ticket for the next
+// launch.  One launch instead of three, the same bits.
+__device__ __forceinline__ void last_block_sums(int m, const double *pdot, double *out_dot, const double *pnorm,
+                                                double *out_norm, unsigned *ticket, double *sh) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (out_dot) {
+    double t = 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) t += __ldcg(pdot + i);
+    t = block_sum(t, sh);
+    if (threadIdx.x == 0) out_dot[0] = t;
+  }
+  if (out_norm) {
+    double t = 0.0;
+    for (int i = threadIdx.x; i < m; i += blockDim.x) t += __ldcg(pnorm + i);
+    t = block_sum(t, sh);
+    if (threadIdx.x == 0) out_norm[0] = t;
+  }
+  if (threadIdx.x == 0) *ticket = 0;
+}
+
+// One fused modified Gram-Schmidt pass over v, its reductions finished in
+// the same launch:
 //   if vprev: v -= h[jprev] * vprev  (the previous projection)
-//   partial_dot  += v . vnext        (the next projection), if vnext
-//   partial_norm += v . v            (if partial_norm)
+//   *out_dot  = v . vnext            (the next projection), if out_dot
+//   *out_norm = v . v                (if out_norm)
 __global__ void __launch_bounds__(kRedThreads)
-k_mgs_pass(long long n, double *__restrict__ v, const double *__restrict__ vprev,
-           const double *__restrict__ hprev, const double *__restrict__ vnext,
-           double *__restrict__ partial_dot, double *__restrict__ partial_norm) {
+k_mgs_pass_sum(long long n, double *__restrict__ v, const double *__restrict__ vprev,
+               const double *__restrict__ hprev, const double *__restrict__ vnext, double *__restrict__ pdot,
+               double *__restrict__ pnorm, double *out_dot, double *out_norm, unsigned *ticket) {
   __shared__ double sh[32];
   const double h = vprev ? *hprev : 0.0;
   double sd = 0.0, sn = 0.0;
@@ -234,14 +264,15 @@ k_mgs_pass(long long n, double *__restrict__ v, const double *__restrict__ vprev
     if (vnext) sd += vi * vnext[i];
     sn += vi * vi;
   }
-  if (partial_dot) {
+  if (out_dot) {
     sd = block_sum(sd, sh);
-    if (threadIdx.x == 0) partial_dot[blockIdx.x] = sd;
+    if (threadIdx.x == 0) pdot[blockIdx.x] = sd;
   }
-  if (partial_norm) {
+  if (out_norm) {
     sn = block_sum(sn, sh);
-    if (threadIdx.x == 0) partial_norm[blockIdx.x] = sn;
+    if (threadIdx.x == 0) pnorm[blockIdx.x] = sn;
   }
+  last_block_sums(gridDim.x, pdot, out_dot, pnorm, out_norm, ticket, sh);
 }
 
 // w = sum_j y[j] V[j]
@@ -295,11 +326,13 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
   const double delta = 1.0e-03;
   DBuf<double> V((size_t)(mr + 1) * n), r(n), w(n), sc(2 * (mr + 2)), dy(mr + 1);
   DBuf<double> pd, pn;
+  DBuf<unsigned> ticket(1);
   Reducer red;
   Precond M{Lu, U, {}};
   const int blocks = red_blocks(n);
   pd.alloc(blocks);
   pn.alloc(blocks);
+  GB_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s));
   double *hs = nullptr;
   GB_CUDA(cudaMallocHost((void **)&hs, 2 * (mr + 2) * sizeof(double)));
   std::unique_ptr<double, void (*)(double *)> hs_guard(hs, [](double *v) { cudaFreeHost(v); });
@@ -347,19 +380,11 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
       for (int j = 0; j <= k + 1; ++j) {
         const double *vprev = j > 0 ? Vj(j - 1) : nullptr;
         const double *vnext = j <= k ? Vj(j) : nullptr;
-        double *pnorm = (j == 0 || j == k + 1) ? pn.p : nullptr;
-        k_mgs_pass<<<blocks, kRedThreads, 0, s>>>(n, v, vprev, sc.p + (j > 0 ? j - 1 : 0), vnext,
-                                                  vnext ? pd.p : nullptr, pnorm);
+        const bool norm = j == 0 || j == k + 1;
+        k_mgs_pass_sum<<<blocks, kRedThreads, 0, s>>>(n, v, vprev, sc.p + (j > 0 ? j - 1 : 0), vnext, pd.p, pn.p,
+                                                      vnext ? sc.p + j : nullptr,
+                                                      norm ? sc.p + (j == 0 ? mr + 1 : k + 1) : nullptr, ticket.p);
         check_launch();
-        if (vnext) {
-          k_reduce_final<<<1, kRedThreads, 0, s>>>(blocks, pd.p, sc.p + j, 0, nullptr);
-          check_launch();
-        }
-        if (pnorm) {
-          k_reduce_final<<<1, kRedThreads, 0, s>>>(blocks, pn.p, sc.p + (j == 0 ? mr + 1 : k + 1), 0,
-                                                   nullptr);
-          check_launch();
-        }
       }
       GB_CUDA(cudaMemcpyAsync(hs, sc.p, (mr + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
       GB_CUDA(cudaStreamSynchronize(s));
@@ -371,17 +396,10 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
         for (int j = 0; j <= k + 1; ++j) {
           const double *vprev = j > 0 ? Vj(j - 1) : nullptr;
           const double *vnext = j <= k ? Vj(j) : nullptr;
-          k_mgs_pass<<<blocks, kRedThreads, 0, s>>>(n, v, vprev, sc.p + (j > 0 ? j - 1 : 0), vnext,
-                                                    vnext ? pd.p : nullptr, j == k + 1 ? pn.p : nullptr);
+          k_mgs_pass_sum<<<blocks, kRedThreads, 0, s>>>(n, v, vprev, sc.p + (j > 0 ? j - 1 : 0), vnext, pd.p,
+                                                        pn.p, vnext ? sc.p + j : nullptr,
+                                                        j == k + 1 ? sc.p + k + 1 : nullptr, ticket.p);
           check_launch();
-          if (vnext) {
-            k_reduce_final<<<1, kRedThreads, 0, s>>>(blocks, pd.p, sc.p + j, 0, nullptr);
-            check_launch();
-          }
-          if (j == k + 1) {
-            k_reduce_final<<<1, kRedThreads, 0, s>>>(blocks, pn.p, sc.p + k + 1, 0, nullptr);
-            check_launch();
-          }
         }
         GB_CUDA(cudaMemcpyAsync(hs, sc.p, (mr + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
         GB_CUDA(cudaStreamSynchronize(s));
