@@ -744,6 +744,18 @@ def main():
         res = plans.pcg(Ac, plan, Pt, bb, xx, tol=1e-10, maxit=2000)
         extras["pcg_c2"] = {"seconds": res.seconds, "iterations": res.iterations, "relres": res.relres,
                             "err_vs_xstar": float(np.linalg.norm(xx.cpu().numpy() - xs) / np.linalg.norm(xs))}
+        # the same PCG on one host core: the restated driver over the
+        # reference's serial kernels (CPU baseline leg only)
+        try:
+            import oracle
+            t0 = time.perf_counter()
+            _, it_c, rel_c = oracle.orc().pcg_ic0(n, A.astuple(), L.astuple(), Lt.astuple(), bb.cpu().numpy(),
+                                                  1e-10, 2000)
+            tc = time.perf_counter() - t0
+            extras["pcg_c2"]["cpu_port"] = {"seconds": tc, "iterations": it_c, "relres": rel_c, "cores": 1,
+                                            "cpu": host_cpu(), "speedup_gpu": tc / res.seconds}
+        except Exception as ex:  # the baseline must not hide the GPU numbers
+            extras["pcg_c2"]["cpu_port"] = {"error": str(ex)}
         # GMRES(30) + right ILU0 on the 96^3 convection-diffusion operator
         from sympiler_gb300._lib import ILU_UNIT_LOWER, ILU_UPPER
         C = mg.convdiff3d(96)
@@ -768,6 +780,18 @@ def main():
             out[prec] = {"seconds": best.seconds, "iterations": best.iterations, "restarts": best.restarts,
                          "relres": best.relres, "status": best.status, "executors": tuned_prec}
         out["speedup_fp32_precond"] = out["f64"]["seconds"] / out["f32"]["seconds"]
+        # the same GMRES on one host core: the restated driver over the
+        # reference's serial kernels and lus_cr (CPU baseline leg only)
+        try:
+            import oracle
+            t0 = time.perf_counter()
+            _, it_c, rel_c = oracle.orc().gmres_ilu0(C.n, C.astuple(), lu.cpu().numpy(), d, bc.cpu().numpy(), 30, 100,
+                                                     1e-10)
+            tc = time.perf_counter() - t0
+            out["cpu_port"] = {"seconds": tc, "iterations": it_c, "relres": rel_c, "cores": 1, "cpu": host_cpu(),
+                               "speedup_gpu_f32": tc / out["f32"]["seconds"]}
+        except Exception as ex:  # the baseline must not hide the GPU numbers
+            out["cpu_port"] = {"error": str(ex)}
         extras["gmres_c3"] = out
         del Cp, dC, lu
         extras["batch_c4"] = bench_batch(dev, stream, flush)
