@@ -62,7 +62,11 @@ enum gbsym_status {
 /* Status of the most recent drop-in call on this host thread. */
 int gbsym_last_error(void);
 const char *gbsym_status_string(int status);
-/* Host buffers returned by the schedule builders; release with gbsym_free. */
+/* Host buffers returned by the schedule builders; release with gbsym_free.
+ * gbsym_alloc gives a buffer of the same kind (NULL for 0 bytes or when
+ * memory is exhausted), for callers that hand buffers back to the library's
+ * owner conventions. */
+void *gbsym_alloc(size_t bytes);
 void gbsym_free(void *p);
 /* Number of kernels this library has launched in this process so far. */
 unsigned long long gbsym_kernel_launches(void);

@@ -97,6 +97,7 @@ SIGNATURES = {
     "gbsym_sn_levels": (_int, [_vp, _vp, _vp]),
     "gbsym_sn_solve": (_int, [_vp, _vp, _int, _int, _vp]),
     "gbsym_sn_check": (_int, [_vp, _vp]),
+    "gbsym_alloc": (_vp, [_sz]),
     "gbsym_sn_selftest_timeout": (_int, [_vp, _ll, _vp]),
     "gbsym_csr_create": (_int, [C.POINTER(_vp), _int, _int, _vp, _vp, _vp, _int, _int, _vp]),
     "gbsym_csr_destroy": (_int, [_vp]),

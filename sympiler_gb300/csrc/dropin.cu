@@ -308,6 +308,7 @@ const char *gbsym_status_string(int status) {
   }
 }
 
+void *gbsym_alloc(size_t bytes) { return bytes ? std::malloc(bytes) : nullptr; }
 void gbsym_free(void *p) { std::free(p); }
 
 unsigned long long gbsym_kernel_launches(void) { return g_launches.load(); }
