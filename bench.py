@@ -362,6 +362,22 @@ def bench_spmv(dev, stream, flush):
         out[name] = {"n": A.n, "nnz": int(A.nnz), "us": t * 1e6, "gbs": byt / t / 1e9,
                      "hbm_frac": byt / t / 1e9 / peak,
                      "fp64_gops": 2 * A.nnz / t / 1e9, "fp64_frac": 2 * A.nnz / t / 1e9 / FP64_PEAK_GOPS}
+        # spmv_csr_parallel on all host cores (CPU baseline leg only)
+        try:
+            import oracle
+            cores = os.cpu_count() or 1
+            xh, yh = x.cpu().numpy(), np.empty(A.n)
+            o = oracle.orc()
+            o.spmv_csr_parallel(A.n, *A.astuple(), xh, yh, cores)
+            tc = []
+            for _ in range(5):
+                t0 = time.perf_counter()
+                o.spmv_csr_parallel(A.n, *A.astuple(), xh, yh, cores)
+                tc.append(time.perf_counter() - t0)
+            out[name]["cpu_port"] = {"us": statistics.median(tc) * 1e6, "cores": cores, "cpu": host_cpu(),
+                                     "speedup_gpu": statistics.median(tc) / t}
+        except Exception as ex:  # the baseline must not hide the GPU numbers
+            out[name]["cpu_port"] = {"error": str(ex)}
         del P
     return out
 
@@ -790,6 +806,12 @@ def main():
             tc = time.perf_counter() - t0
             out["cpu_port"] = {"seconds": tc, "iterations": it_c, "relres": rel_c, "cores": 1, "cpu": host_cpu(),
                                "speedup_gpu_f32": tc / out["f32"]["seconds"]}
+            # one ILU0 apply (lus_cr) on one core, beside the GPU's
+            luh = lu.cpu().numpy()
+            rh = bc.cpu().numpy()
+            t0 = time.perf_counter()
+            oracle.orc().lus_cr(C.n, C.p, C.i, luh, d, rh)
+            out["cpu_port"]["lus_cr_ms"] = (time.perf_counter() - t0) * 1e3
         except Exception as ex:  # the baseline must not hide the GPU numbers
             out["cpu_port"] = {"error": str(ex)}
         extras["gmres_c3"] = out
