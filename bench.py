@@ -340,8 +340,9 @@ def bench_batch(dev, stream, flush, nsys=512, k=8):
 
 def bench_spmv(dev, stream, flush):
     """CSR SpMV y = A x (the Krylov drivers' system product) on the C3 and C2
-    operators, FP64, L2 flushed before every timed call.  Bytes are the
-    survey's B_spmv = (V + 4) nnz + 4 (n + 1) + 2 S n."""
+    operators, FP64, L2 flushed before every timed call.  Bytes are
+    B_spmv = (V + 4) nnz + 4 (n + 1) + 2 S n: every stored value and index
+    read once, x read and y written once."""
     import torch
     from sympiler_gb300 import matgen as mg
     from sympiler_gb300.plans import CsrPlan

@@ -4,7 +4,7 @@ Two shared libraries:
 
 * ``oracle/_build/liboracle.so`` -- the project's C restatement
   (``oracle/oracle.c``).  Built everywhere, including the GPU host, since it
-  is the checker for the parity tests and the CPU baseline of the benchmark.
+  is the oracle of the parity tests and the CPU baseline of the benchmark.
 * ``oracle/_ref/libsymref.so`` -- the reference's own C++ executors,
   compiled in place from the sympiler/sympiler source tree (never copied)
   together with ``oracle/ref_capi.cpp`` and the project-written

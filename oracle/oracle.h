@@ -3,7 +3,7 @@
  * executor path (sympiler/sympiler, namespace sym_lib).
  *
  * TEST INFRASTRUCTURE ONLY.  Nothing in the product library links, loads or
- * calls this code.  It is the checker the GPU path is compared against: the
+ * calls this code.  It is the oracle the GPU path is compared against: the
  * parity tests, the smoke check and the CPU-baseline leg of the benchmark are
  * its only users.
  *
