@@ -104,23 +104,26 @@ __device__ __forceinline__ T ldv(const T *p) {
 // Static part of a row: everything that does not depend on x.  All loads
 // are independent of each other (slab entries are addressed by the packed
 // row index alone), so they are in flight together.
-template <class T>
+// S is the slab capacity the registers hold; it must be at least A.K.  A
+// kernel compiled for a narrow slab (S = 4 covers every stencil factor up
+// to three off-diagonals per row) keeps far fewer registers live.
+template <class T, int S = kSlabMax>
 struct RowStatic {
   int orig, len, ovb;
   T d, y;
-  int c[kSlabMax];
-  T v[kSlabMax];
+  int c[S];
+  T v[S];
 };
 
-template <class T>
-__device__ __forceinline__ void load_row(const TriView<T> &A, int row, RowStatic<T> &r) {
+template <class T, int S>
+__device__ __forceinline__ void load_row(const TriView<T> &A, int row, RowStatic<T, S> &r) {
   r.orig = A.perm[row];
   r.len = A.len[row];
   r.d = A.dg ? A.dg[row] : T(1);
   r.y = A.dg ? A.rc[row] : T(1);
   r.ovb = A.ovp ? A.ovp[row] : 0;
 #pragma unroll
-  for (int q = 0; q < kSlabMax; ++q)
+  for (int q = 0; q < S; ++q)
     if (q < A.K) {
       r.c[q] = A.sci[(size_t)q * A.npad + row];
       r.v[q] = A.sv[(size_t)q * A.npad + row];
@@ -146,8 +149,8 @@ __device__ __forceinline__ T row_accumulate(const TriView<T> &A, const RowStatic
   return acc;
 }
 
-template <class T>
-__device__ __forceinline__ T row_finish(const TriView<T> &A, const RowStatic<T> &r, T acc) {
+template <class T, int S>
+__device__ __forceinline__ T row_finish(const TriView<T> &A, const RowStatic<T, S> &r, T acc) {
   return A.dg ? div_by(acc, r.d, r.y) : acc;
 }
 

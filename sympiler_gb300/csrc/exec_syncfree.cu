@@ -123,8 +123,10 @@ __device__ __forceinline__ int deal_warp(int nsm) {
 // slice reads -- a loop with no floating-point work, so polling rounds cost
 // the FP64 pipe nothing -- and then each lane computes and publishes its
 // slice once, in storage order.
-template <class T, int G, int VEC, int AR>
-__global__ void __launch_bounds__(kSfBlock)
+// A narrow slab (KS = 4) fits in 80 registers without spilling, which lets
+// three blocks share an SM; the full slab keeps the compiler's choice.
+template <class T, int G, int VEC, int AR, int KS>
+__global__ void __launch_bounds__(kSfBlock, KS <= 4 ? 3 : 1)
 k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int *__restrict__ unit_row,
            const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
   constexpr unsigned FULL = 0xffffffffu;
@@ -137,13 +139,13 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
   for (int u = warp; u < nunits; u += nwarps) {
     const bool active = sub < unit_cnt[u];
     const int row = unit_row[u] + sub;
-    RowStatic<T> rs;
+    RowStatic<T, KS> rs;
     if (active) load_row(A, row, rs);
     const int ns = active ? min(rs.len, A.K) : 0;
     for (int sl = 0; sl < nslices; ++sl) {
       const int r = gl * VEC + sl * G * VEC;
       bool done = !(active && r < k);
-      T xv[kSlabMax][VEC];
+      T xv[KS][VEC];
       unsigned got = 0;
       const unsigned need = (1u << ns) - 1u;
       int jo = A.K;          // next overflow dependency
@@ -159,16 +161,16 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
       // copies (a copy would wait for the loads).  Wider lanes keep a single
       // round: the second buffer's registers would halve their occupancy.
       constexpr bool kTwoRounds = VEC == 1;
-      T va[kSlabMax][VEC], vb[kSlabMax][VEC];
-      auto issue = [&](T (&buf)[kSlabMax][VEC]) {
+      T va[KS][VEC], vb[KS][VEC];
+      auto issue = [&](T (&buf)[KS][VEC]) {
 #pragma unroll
-        for (int q = 0; q < kSlabMax; ++q)
+        for (int q = 0; q < KS; ++q)
           if (q < ns && !((got >> q) & 1u)) ld_rlx<T, VEC>(y + (size_t)rs.c[q] * k + r, buf[q]);
       };
-      auto absorb = [&](T (&buf)[kSlabMax][VEC]) {
+      auto absorb = [&](T (&buf)[KS][VEC]) {
         bool moved = false;
 #pragma unroll
-        for (int q = 0; q < kSlabMax; ++q)
+        for (int q = 0; q < KS; ++q)
           if (q < ns && !((got >> q) & 1u) && all_ready<T, VEC>(buf[q])) {
 #pragma unroll
             for (int w = 0; w < VEC; ++w) xv[q][w] = buf[q][w];
@@ -215,7 +217,7 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
       }
       if (active && r < k) {
 #pragma unroll
-        for (int q = 0; q < kSlabMax; ++q)
+        for (int q = 0; q < KS; ++q)
           if (q < ns) {
 #pragma unroll
             for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], rs.v[q], xv[q][w]);
@@ -245,9 +247,14 @@ template <class K, class... Args>
 static void launch_coop(gbsym_tri_s *t, int k_of_launch, K kernel, cudaStream_t s, Args... args) {
   int per_sm = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kSfBlock, 0));
-  // fewer resident warps poll less: one block per SM measured best for one
-  // right-hand side, two for many
-  const int want = t->sf_blocks_per_sm > 0 ? t->sf_blocks_per_sm : (k_of_launch > 1 ? 2 : 1);
+  // fewer resident warps poll less, more hide the FP64 chain: one block per
+  // SM measured best for one right-hand side, two for a few, three (where
+  // the registers allow) for 32 and more (C2 factor: 262 us at one RHS;
+  // 277 / 279 / 310 us at 8 RHS and 974 / 573 / 500 us at 64 RHS with
+  // one / two / three blocks)
+  int want = t->sf_blocks_per_sm;
+  if (want <= 0) want = t->sf_bps_tuned[k_of_launch > 1 ? 1 : 0];
+  if (want <= 0) want = k_of_launch == 1 ? 1 : (k_of_launch < 32 ? 2 : 3);
   const int grid = std::max(1, std::min(per_sm, want)) * num_sms();
   void *params[] = {(void *)&args...};
   GB_CUDA(cudaLaunchCooperativeKernel((const void *)kernel, dim3(grid), dim3(kSfBlock), params, 0, s));
@@ -282,8 +289,10 @@ static Units sf_units(gbsym_tri_s *t, int rpw) {
   return {b.row.p, b.cnt.p, b.n};
 }
 
-template <class T, int G, int AR>
-static void sf_g(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
+// KS: slab capacity compiled into the kernel's registers (4 when the plan's
+// slab is at most four wide, as for every stencil factor, else the maximum).
+template <class T, int G, int AR, int KS>
+static void sf_gk(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   const TriView<T> A = view_of<T>(t);
   const Units U = sf_units(t, 32 / G);
   // FP64 takes one value per lane: the polling then keeps two rounds of
@@ -293,12 +302,20 @@ static void sf_g(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   const bool v4 = sizeof(T) == 4 && (k % 4 == 0) && ((uintptr_t)x % 16 == 0);
   const bool v2 = sizeof(T) == 4 && (k % 2 == 0) && ((uintptr_t)x % (2 * sizeof(T)) == 0);
   if (v4)
-    launch_coop(t, k, k_syncfree<T, G, (sizeof(T) == 4 ? 4 : 2), AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal,
+    launch_coop(t, k, k_syncfree<T, G, (sizeof(T) == 4 ? 4 : 2), AR, KS>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal,
                 t->err.p);
   else if (v2)
-    launch_coop(t, k, k_syncfree<T, G, 2, AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+    launch_coop(t, k, k_syncfree<T, G, 2, AR, KS>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
   else
-    launch_coop(t, k, k_syncfree<T, G, 1, AR>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+    launch_coop(t, k, k_syncfree<T, G, 1, AR, KS>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+}
+
+template <class T, int G, int AR>
+static void sf_g(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
+  if (t->K <= 4)
+    sf_gk<T, G, AR, 4>(t, x, y, k, s);
+  else
+    sf_gk<T, G, AR, kSlabMax>(t, x, y, k, s);
 }
 
 template <class T, int AR>
