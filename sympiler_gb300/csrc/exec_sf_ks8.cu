@@ -1,0 +1,10 @@
+// exec_sf_ks8.cu -- the sync-free sweep's kernels compiled for a full (kSlabMax-entry)
+// slab (plans with t->K > 4).
+#include "exec_syncfree_kernel.cuh"
+
+namespace gbsym {
+
+template void sf_run_ks<double, kSlabMax>(gbsym_tri_s *, double *, double *, int, cudaStream_t);
+template void sf_run_ks<float, kSlabMax>(gbsym_tri_s *, float *, float *, int, cudaStream_t);
+
+}  // namespace gbsym

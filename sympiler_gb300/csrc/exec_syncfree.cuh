@@ -1,0 +1,27 @@
+// exec_syncfree.cuh -- declarations shared by the SYNCFREE executor's host
+// side (exec_syncfree.cu) and its kernels.  The kernels are compiled once
+// per slab width, each width in its own translation unit (exec_sf_ks*.cu),
+// so that the widths build in parallel.
+#pragma once
+
+#include "exec_common.cuh"
+
+namespace gbsym {
+
+constexpr int kSfBlock = 256;
+
+// Warp units of `rpw` rows cut per level: unit u covers packed rows
+// row[u] .. row[u] + cnt[u], all in one level.  Built once per rows-per-unit.
+struct Units {
+  const int *row, *cnt;
+  int n;
+};
+
+Units sf_units(gbsym_tri_s *t, int rpw);
+
+// The sweep of a plan whose slab is at most KS entries wide (KS >= t->K),
+// into the sentinel-filled scratch y.
+template <class T, int KS>
+void sf_run_ks(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s);
+
+}  // namespace gbsym

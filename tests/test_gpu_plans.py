@@ -189,6 +189,45 @@ def test_long_rows_every_executor(gpu, orc, exec_mode):
     assert np.array_equal(x32.cpu().numpy(), ref32)
 
 
+def _banded_lower(n, w, seed):
+    """Lower triangle with w sub-diagonals: every row past the first w holds
+    exactly w off-diagonals, so the plan's slab is w entries wide."""
+    import scipy.sparse as sp
+    rng = np.random.default_rng(seed)
+    offs = list(range(0, -w - 1, -1))
+    diags = [1.0 + rng.uniform(0.0, 1.0, n)] + [rng.uniform(-1.0, 1.0, n - d) / (w + 1) for d in range(1, w + 1)]
+    return mg.from_scipy(sp.diags(diags, offs, shape=(n, n), format="csr"))
+
+
+@pytest.mark.parametrize("w", [1, 2, 3, 4, 5, 8])
+def test_syncfree_every_slab_width(gpu, orc, w):
+    """The sync-free sweep is compiled once per slab width (2, 3, 4 and the
+    full 8); each width's kernels match the oracle bit for bit in FP64 at 1,
+    8 and 64 right-hand sides and in FP32 at one."""
+    from sympiler_gb300._lib import EXEC_SYNCFREE
+    from sympiler_gb300.plans import TriPlan
+    L = _banded_lower(4099, w, seed=w)
+    plan = TriPlan(L.n, *L.astuple())
+    plan.set_exec(EXEC_SYNCFREE)
+    rng = np.random.default_rng(100 + w)
+    for k in (1, 8, 64):
+        B = rng.standard_normal((L.n, k))
+        ref = _oracle_mrhs(orc, L, B)
+        x = torch.from_numpy(B.copy()).cuda()
+        plan.solve(x if k > 1 else x.view(-1))
+        plan.check()
+        assert np.array_equal(x.cpu().numpy(), ref), (w, k)
+    p32 = TriPlan(L.n, *L.astuple(), dtype="f32")
+    p32.set_exec(EXEC_SYNCFREE)
+    b32 = rng.standard_normal(L.n).astype(np.float32)
+    ref32 = b32.copy()
+    orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), ref32)
+    x32 = torch.from_numpy(b32.copy()).cuda()
+    p32.solve(x32)
+    p32.check()
+    assert np.array_equal(x32.cpu().numpy(), ref32), w
+
+
 def test_autotune_picks_a_working_executor(gpu, orc, c2_factor):
     from sympiler_gb300.plans import TriPlan
     _, L, _ = c2_factor
