@@ -140,6 +140,25 @@ void gbsym_spilu0_csr(int n, int nnz, const int *Ap, const int *Ai,
                       const double *Ax, const int *A_diag, double *l);
 /* sparse_blas/spic0.cpp:106-128 ; sparse_blas_lib.h:242 (upper CSR of A, in place) */
 void gbsym_spic0_csr(int n, double *val, int *rowPtr, int *rowIdx);
+/* sparse_blas/spilu0.cpp:54-106 ; sparse_blas_lib.h:279-282.  The LBC
+ * schedule (level_ptr into par_ptr into partition) is validated against
+ * the dependencies of the rows (entries left of each diagonal); an invalid
+ * one records GBSYM_ERR_BAD_SCHEDULE and leaves l untouched.  ILU0's row
+ * sequence does not depend on the schedule, so l equals gbsym_spilu0_csr's
+ * bit for bit.  tempvecs (the reference's per-thread scratch) is not used. */
+void gbsym_spilu0_csr_lbc(int n, int nnz, const int *Ap, const int *Ai,
+                          const double *Ax, const int *A_diag, double *l,
+                          int level_no, const int *level_ptr,
+                          const int *par_ptr, const int *partition,
+                          int *tempvecs);
+/* sparse_blas/spic0.cpp:130-160 ; sparse_blas_lib.h:243-245.  The schedule
+ * is over the columns of L (rows of the upper CSR) and is validated against
+ * the solve DAG of L.  The reference subtracts under `omp atomic`, so its
+ * result depends on thread timing; this one applies every update in
+ * gbsym_spic0_csr's (serial) order and equals it bit for bit. */
+void gbsym_spic0_csr_lbc(int n, double *val, int *rowPtr, int *colIdx,
+                         int level_no, int *level_ptr, int *par_ptr,
+                         int *partition);
 /* sparse_blas/parsy/gmres/mgmres.cpp:598-689 ; include/sympiler/parsy/gmres/mgmres.hpp:41 */
 void gbsym_parsy_lus_cr(int n, int nz_num, int *ia, int *ja, double *l,
                         int *ua, double *r, double *z);

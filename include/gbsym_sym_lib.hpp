@@ -80,13 +80,23 @@ inline int ltsolve(int n, int *Lp, int *Li, double *Lx, double *x) {
   return gbsym_ltsolve(n, Lp, Li, Lx, x);
 }
 
-// ---- factor producers (sparse_blas_lib.h:242, 276-277) ---------------------------
+// ---- factor producers (sparse_blas_lib.h:242-245, 276-282) ------------------------
 inline void spic0_csr(int n, double *val, int *rowPtr, int *rowIdx) {
   gbsym_spic0_csr(n, val, rowPtr, rowIdx);
 }
 inline void spilu0_csr(int n, int nnz, const int *Ap, const int *Ai, const double *Ax,
                        const int *A_diag, double *l) {
   gbsym_spilu0_csr(n, nnz, Ap, Ai, Ax, A_diag, l);
+}
+inline void spic0_csr_lbc(int n, double *val, int *rowPtr, int *colIdx, int level_no,
+                          int *level_ptr, int *par_ptr, int *partition) {
+  gbsym_spic0_csr_lbc(n, val, rowPtr, colIdx, level_no, level_ptr, par_ptr, partition);
+}
+inline void spilu0_csr_lbc(int n, int nnz, const int *Ap, const int *Ai, const double *Ax,
+                           const int *A_diag, double *l, int level_no, const int *level_ptr,
+                           const int *par_ptr, const int *partition, int *tempvecs) {
+  gbsym_spilu0_csr_lbc(n, nnz, Ap, Ai, Ax, A_diag, l, level_no, level_ptr, par_ptr, partition,
+                       tempvecs);
 }
 
 // ---- schedule builder at the reference's build_levelSet_CSC call sites ------------

@@ -182,6 +182,8 @@ class _Ref:
         self.spmv_csr_parallel = b("ref_spmv_csr_parallel", None, [_int, _i, _i, _d, _d, _d])
         self._spilu0 = b("ref_spilu0_csr", None, [_int, _int, _i, _i, _d, _i, _d])
         self._spic0 = b("ref_spic0_csr", None, [_int, _d, _i, _i])
+        self._spilu0_lbc = b("ref_spilu0_csr_lbc", None, [_int, _int, _i, _i, _d, _i, _d, _int, _i, _i, _i])
+        self._spic0_lbc = b("ref_spic0_csr_lbc", None, [_int, _d, _i, _i, _int, _i, _i, _i])
         self._lus_cr = b("ref_lus_cr", None, [_int, _int, _i, _i, _d, _i, _d, _d])
         self._tree_lvl = b("ref_tree_levelset", _int, [_int, _i, _i, _i])
         self._coarse6 = b("ref_coarse_levelset6", _int,
@@ -218,6 +220,18 @@ class _Ref:
         Ui_pad = np.concatenate([Ui, np.array([n], dtype=np.int32)])
         v = np.array(Ux, dtype=np.float64, copy=True)
         self._spic0(n, v, Up, Ui_pad)
+        return v
+
+    def spilu0_csr_lbc(self, n, Ap, Ai, Ax, A_diag, level_no, lp, pp, part):
+        l = np.empty_like(Ax)
+        self._spilu0_lbc(n, int(Ap[n]), Ap, Ai, Ax, A_diag, l, level_no, lp, pp, part)
+        return l
+
+    def spic0_csr_lbc(self, n, Up, Ui, Ux, level_no, lp, pp, part):
+        # padded like spic0_csr: the reference reads one index past a row
+        Ui_pad = np.concatenate([Ui, np.array([n], dtype=np.int32)])
+        v = np.array(Ux, dtype=np.float64, copy=True)
+        self._spic0_lbc(n, v, Up, Ui_pad, level_no, lp, pp, part)
         return v
 
     def lus_cr(self, n, ia, ja, l, ua, r):

@@ -13,8 +13,11 @@
  * They are defined below as stubs that abort, so the library links with no
  * undefined symbols.
  */
+#include <omp.h>
+
 #include <cstdio>
 #include <cstdlib>
+#include <vector>
 
 #include "sympiler/sparse_blas_lib.h"
 #include "sympiler/parsy/gmres/mgmres.hpp"
@@ -140,6 +143,21 @@ void ref_spilu0_csr(int n, int nnz, const int *Ap, const int *Ai,
 }
 void ref_spic0_csr(int n, double *val, int *rowPtr, int *rowIdx) {
   spic0_csr(n, val, rowPtr, rowIdx);
+}
+// The reference's per-thread scratch: n ints per OpenMP thread (its thread
+// number picks the slice), all -1, as its header asks.
+void ref_spilu0_csr_lbc(int n, int nnz, const int *Ap, const int *Ai,
+                        const double *Ax, const int *A_diag, double *l,
+                        int level_no, const int *level_ptr, const int *par_ptr,
+                        const int *partition) {
+  std::vector<int> tmp((size_t)n * (omp_get_max_threads() + 1), -1);
+  spilu0_csr_lbc(n, nnz, Ap, Ai, Ax, A_diag, l, level_no, level_ptr, par_ptr,
+                 partition, tmp.data());
+}
+void ref_spic0_csr_lbc(int n, double *val, int *rowPtr, int *colIdx,
+                       int level_no, int *level_ptr, int *par_ptr,
+                       int *partition) {
+  spic0_csr_lbc(n, val, rowPtr, colIdx, level_no, level_ptr, par_ptr, partition);
 }
 void ref_lus_cr(int n, int nz_num, int *ia, int *ja, double *l, int *ua,
                 double *r, double *z) {

@@ -53,6 +53,8 @@ SIGNATURES = {
     "gbsym_spmv_csr_parallel": (None, [_int, _vp, _vp, _vp, _vp, _vp]),
     "gbsym_spilu0_csr": (None, [_int, _int, _vp, _vp, _vp, _vp, _vp]),
     "gbsym_spic0_csr": (None, [_int, _vp, _vp, _vp]),
+    "gbsym_spilu0_csr_lbc": (None, [_int, _int, _vp, _vp, _vp, _vp, _vp, _int, _vp, _vp, _vp, _vp]),
+    "gbsym_spic0_csr_lbc": (None, [_int, _vp, _vp, _vp, _int, _vp, _vp, _vp]),
     "gbsym_parsy_lus_cr": (None, [_int, _int, _vp, _vp, _vp, _vp, _vp, _vp]),
     "gbsym_build_levelset_csc": (_int, [_int, _vp, _vp, _ppi, _ppi]),
     "gbsym_build_levelset_csr": (_int, [_int, _vp, _vp, _ppi, _ppi]),

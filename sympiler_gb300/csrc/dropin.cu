@@ -461,45 +461,99 @@ void gbsym_spmv_csr_parallel(int n, const int *Ap, const int *Ai, const double *
 }
 
 // ---- factor producers and the ILU apply -----------------------------------
+// ILU0 of the CSR (Ap, Ai, Ax) with diagonal positions A_diag into l, on the
+// GPU.  With an LBC schedule, the schedule is first checked against the
+// rows' dependencies (the entries left of each diagonal); ILU0's arithmetic
+// per row does not depend on the order rows run in, so the factor is the
+// same either way.
+static void ilu0_dropin(int n, int nnz, const int *Ap, const int *Ai, const double *Ax,
+                        const int *A_diag, double *l, const HostLbc *lbc) {
+  GB_CHECK(n >= 0, GBSYM_ERR_SIZE);
+  if (n == 0) return;
+  GB_CHECK(Ap && Ai && Ax && A_diag && l, GBSYM_ERR_NULL_ARG);
+  GB_CHECK(nnz == Ap[n], GBSYM_ERR_BAD_MATRIX);
+  cudaStream_t s = thread_stream();
+  DBuf<int> dp, di, dd;
+  DBuf<double> dx, dl(nnz);
+  upload(dp, Ap, n + 1, false, s);
+  upload(di, Ai, nnz, false, s);
+  upload(dx, Ax, nnz, false, s);
+  upload(dd, A_diag, n, false, s);
+  if (lbc) {
+    validate_matrix(n, dp.p, di.p, dd.p, GBSYM_ILU_UNIT_LOWER, s);
+    validate_lbc(n, dp.p, di.p, dd.p, GBSYM_ILU_UNIT_LOWER, lbc->level_no, lbc->level_ptr, lbc->par_ptr,
+                 lbc->partition, s);
+  }
+  int st = guarded([&] { ilu0_device(n, dp.p, di.p, dx.p, dd.p, dl.p, s); });
+  if (st == GBSYM_ERR_BAD_MATRIX) throw Err{st};
+  GB_CUDA(cudaMemcpyAsync(l, dl.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  if (st) throw Err{st};
+}
+
+// IC0 in place on the upper CSR of A (diagonal first in each row), on the
+// GPU.  With an LBC schedule over the columns of L, the schedule is first
+// checked against the solve DAG of L: column c must come after every column
+// i whose row of the upper CSR holds c.  The updates are applied in the
+// serial order whatever the schedule.
+static void ic0_dropin(int n, double *val, const int *rowPtr, const int *colIdx, const HostLbc *lbc) {
+  GB_CHECK(n >= 0, GBSYM_ERR_SIZE);
+  if (n == 0) return;
+  GB_CHECK(val && rowPtr && colIdx, GBSYM_ERR_NULL_ARG);
+  cudaStream_t s = thread_stream();
+  const int nnz = rowPtr[n];
+  GB_CHECK(nnz >= 0, GBSYM_ERR_BAD_MATRIX);
+  DBuf<int> dp, di;
+  DBuf<double> dv;
+  if (lbc) {
+    // structure first, on the host, before any kernel indexes with it
+    GB_CHECK(rowPtr[0] == 0, GBSYM_ERR_BAD_MATRIX);
+    for (int r = 0; r < n; ++r) {
+      GB_CHECK(rowPtr[r] < rowPtr[r + 1] && colIdx[rowPtr[r]] == r, GBSYM_ERR_BAD_MATRIX);
+      for (int e = rowPtr[r] + 1; e < rowPtr[r + 1]; ++e)
+        GB_CHECK(colIdx[e] > r && colIdx[e] < n, GBSYM_ERR_BAD_MATRIX);
+    }
+  }
+  upload(dp, rowPtr, n + 1, false, s);
+  upload(di, colIdx, nnz, false, s);
+  upload(dv, val, nnz, false, s);
+  if (lbc) {
+    Transposed L;  // CSR of L: row c lists the columns i <= c, diagonal last
+    transpose_pattern(n, nnz, dp.p, di.p, L, s);
+    validate_lbc(n, L.rp.p, L.ci.p, nullptr, GBSYM_LOWER_DIAG_LAST, lbc->level_no, lbc->level_ptr,
+                 lbc->par_ptr, lbc->partition, s);
+  }
+  int st = guarded([&] { ic0_device(n, dv.p, dp.p, di.p, s); });
+  if (st == GBSYM_ERR_BAD_MATRIX) throw Err{st};
+  GB_CUDA(cudaMemcpyAsync(val, dv.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+  if (st) throw Err{st};
+}
+
 void gbsym_spilu0_csr(int n, int nnz, const int *Ap, const int *Ai, const double *Ax,
                       const int *A_diag, double *l) {
+  record([&] { ilu0_dropin(n, nnz, Ap, Ai, Ax, A_diag, l, nullptr); });
+}
+
+void gbsym_spilu0_csr_lbc(int n, int nnz, const int *Ap, const int *Ai, const double *Ax,
+                          const int *A_diag, double *l, int level_no, const int *level_ptr,
+                          const int *par_ptr, const int *partition, int *tempvecs) {
+  (void)tempvecs;
   record([&] {
-    GB_CHECK(n >= 0, GBSYM_ERR_SIZE);
-    if (n == 0) return;
-    GB_CHECK(Ap && Ai && Ax && A_diag && l, GBSYM_ERR_NULL_ARG);
-    GB_CHECK(nnz == Ap[n], GBSYM_ERR_BAD_MATRIX);
-    cudaStream_t s = thread_stream();
-    DBuf<int> dp, di, dd;
-    DBuf<double> dx, dl(nnz);
-    upload(dp, Ap, n + 1, false, s);
-    upload(di, Ai, nnz, false, s);
-    upload(dx, Ax, nnz, false, s);
-    upload(dd, A_diag, n, false, s);
-    int st = guarded([&] { ilu0_device(n, dp.p, di.p, dx.p, dd.p, dl.p, s); });
-    if (st == GBSYM_ERR_BAD_MATRIX) throw Err{st};
-    GB_CUDA(cudaMemcpyAsync(l, dl.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
-    GB_CUDA(cudaStreamSynchronize(s));
-    if (st) throw Err{st};
+    HostLbc lbc{level_no, level_ptr, par_ptr, partition};
+    ilu0_dropin(n, nnz, Ap, Ai, Ax, A_diag, l, n ? &lbc : nullptr);
   });
 }
 
 void gbsym_spic0_csr(int n, double *val, int *rowPtr, int *rowIdx) {
+  record([&] { ic0_dropin(n, val, rowPtr, rowIdx, nullptr); });
+}
+
+void gbsym_spic0_csr_lbc(int n, double *val, int *rowPtr, int *colIdx, int level_no, int *level_ptr,
+                         int *par_ptr, int *partition) {
   record([&] {
-    GB_CHECK(n >= 0, GBSYM_ERR_SIZE);
-    if (n == 0) return;
-    GB_CHECK(val && rowPtr && rowIdx, GBSYM_ERR_NULL_ARG);
-    cudaStream_t s = thread_stream();
-    const int nnz = rowPtr[n];
-    DBuf<int> dp, di;
-    DBuf<double> dv;
-    upload(dp, rowPtr, n + 1, false, s);
-    upload(di, rowIdx, nnz, false, s);
-    upload(dv, val, nnz, false, s);
-    int st = guarded([&] { ic0_device(n, dv.p, dp.p, di.p, s); });
-    if (st == GBSYM_ERR_BAD_MATRIX) throw Err{st};
-    GB_CUDA(cudaMemcpyAsync(val, dv.p, nnz * sizeof(double), cudaMemcpyDeviceToHost, s));
-    GB_CUDA(cudaStreamSynchronize(s));
-    if (st) throw Err{st};
+    HostLbc lbc{level_no, level_ptr, par_ptr, partition};
+    ic0_dropin(n, val, rowPtr, colIdx, n ? &lbc : nullptr);
   });
 }
 

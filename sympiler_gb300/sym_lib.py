@@ -368,6 +368,32 @@ def spic0_csr(n, val, rowPtr, rowIdx):  # noqa: N803
     _raise_last("spic0_csr")
 
 
+def spilu0_csr_lbc(n, nnz, Ap, Ai, Ax, A_diag, l, level_no, level_ptr, par_ptr, partition, tempvecs=None):
+    """sparse_blas/spilu0.cpp:54-106 -- the schedule is validated, then l
+    receives the packed ILU0 factor (equal to spilu0_csr's); ``tempvecs``
+    (per-thread scratch) is unused."""
+    Ap, Ai, Ax = _arr(Ap, _I32, "Ap"), _arr(Ai, _I32, "Ai"), _arr(Ax, _F64, "Ax")
+    A_diag = _arr(A_diag, _I32, "A_diag")
+    lp, pp, pa = (_arr(a, _I32, nm) for a, nm in ((level_ptr, "level_ptr"), (par_ptr, "par_ptr"),
+                                                   (partition, "partition")))
+    l = _arr(l, _F64, "l", True)
+    lib().gbsym_spilu0_csr_lbc(n, nnz, _p(Ap), _p(Ai), _p(Ax), _p(A_diag), _p(l), level_no, _p(lp), _p(pp),
+                               _p(pa), None)
+    _raise_last("spilu0_csr_lbc")
+
+
+def spic0_csr_lbc(n, val, rowPtr, colIdx, level_no, level_ptr, par_ptr, partition):  # noqa: N803
+    """sparse_blas/spic0.cpp:130-160 -- IC0 in place on the upper CSR of A
+    under a validated LBC schedule over the columns of L; the result equals
+    spic0_csr's bit for bit."""
+    val = _arr(val, _F64, "val", True)
+    rowPtr, colIdx = _arr(rowPtr, _I32, "rowPtr"), _arr(colIdx, _I32, "colIdx")
+    lp, pp, pa = (_arr(a, _I32, nm) for a, nm in ((level_ptr, "level_ptr"), (par_ptr, "par_ptr"),
+                                                   (partition, "partition")))
+    lib().gbsym_spic0_csr_lbc(n, _p(val), _p(rowPtr), _p(colIdx), level_no, _p(lp), _p(pp), _p(pa))
+    _raise_last("spic0_csr_lbc")
+
+
 # ---- schedule builders ----------------------------------------------------
 
 def _levels(fn, n, p, i, where):

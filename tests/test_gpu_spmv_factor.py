@@ -106,3 +106,68 @@ def test_ic0_pivot_error(gpu):
     with pytest.raises(GbsymError) as e:
         sym_lib.spic0_csr(U.n, v, U.p, U.i)
     assert e.value.status == ERR_PIVOT
+
+
+def _lbc_of_lower(n, p, i, parts):
+    """The library's DAG LBC inspector on a lower CSR pattern (diagonal last),
+    as the reference demo calls get_coarse_levelSet_DAG_CSC_tree."""
+    from sympiler_gb300 import sym_lib
+    nl, lp, pn, pp, nodes = sym_lib.get_coarse_levelSet_DAG_CSC_tree(n, p, i, 0, parts, -1, 100)
+    return nl, lp, pp, nodes
+
+
+@pytest.mark.parametrize("parts", [2, 8])
+def test_spilu0_csr_lbc_drop_in(gpu, orc, parts):
+    """spilu0_csr_lbc under a valid LBC schedule of the rows' dependencies
+    equals the serial oracle bit for bit (ILU0's row arithmetic does not
+    depend on the schedule); a schedule that runs a row before one it reads
+    is refused and leaves l untouched."""
+    from sympiler_gb300 import sym_lib
+    from sympiler_gb300._lib import ERR_BAD_SCHEDULE, GbsymError
+    for A in (mg.convdiff3d(12), mg.convdiff3d(7)):
+        d = mg.diag_ptr(A)
+        ref, ok = orc.spilu0_csr(A.n, A.p, A.i, A.x, d)
+        assert ok
+        Lpat = mg.tril(A)  # dependencies of row i: its entries left of the diagonal
+        nl, lp, pp, nodes = _lbc_of_lower(A.n, Lpat.p, Lpat.i, parts)
+        l = np.zeros_like(A.x)
+        sym_lib.spilu0_csr_lbc(A.n, A.nnz, A.p, A.i, A.x, d, l, nl, lp, pp, nodes)
+        assert np.array_equal(l, ref)
+    bad = np.arange(A.n, dtype=np.int32)[::-1].copy()  # last row first: violates every dependency
+    l = np.full_like(A.x, 7.0)
+    with pytest.raises(GbsymError) as e:
+        sym_lib.spilu0_csr_lbc(A.n, A.nnz, A.p, A.i, A.x, d, l, 1, np.array([0, 1], np.int32),
+                               np.array([0, A.n], np.int32), bad)
+    assert e.value.status == ERR_BAD_SCHEDULE
+    assert np.all(l == 7.0)
+
+
+@pytest.mark.parametrize("parts", [2, 8])
+def test_spic0_csr_lbc_drop_in(gpu, orc, parts):
+    """spic0_csr_lbc under a valid LBC schedule over the columns of L equals
+    the serial spic0_csr (oracle and fixtures) bit for bit; an invalid
+    schedule is refused and leaves val untouched."""
+    from sympiler_gb300 import sym_lib
+    from sympiler_gb300._lib import ERR_BAD_SCHEDULE, GbsymError
+    for name in ("ic0_lap3d_10", "ic0_random_spd_2000"):
+        g = golden(name)
+        n = len(g["Up"]) - 1
+        L = mg.transpose(mg.CSR(n, g["Up"], g["Ui"], g["Ux"]))  # CSR of L: the solve DAG of the columns
+        nl, lp, pp, nodes = _lbc_of_lower(n, L.p, L.i, parts)
+        v = g["Ux"].copy()
+        sym_lib.spic0_csr_lbc(n, v, g["Up"], g["Ui"], nl, lp, pp, nodes)
+        assert np.array_equal(v, g["factor"]), name
+    A = mg.lap3d(16, 1e-2)
+    U = mg.triu(A)
+    ref, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+    L = mg.transpose(U)
+    nl, lp, pp, nodes = _lbc_of_lower(U.n, L.p, L.i, parts)
+    v = U.x.copy()
+    sym_lib.spic0_csr_lbc(U.n, v, U.p, U.i, nl, lp, pp, nodes)
+    assert np.array_equal(v, ref)
+    bad = np.arange(U.n, dtype=np.int32)[::-1].copy()
+    v = U.x.copy()
+    with pytest.raises(GbsymError) as e:
+        sym_lib.spic0_csr_lbc(U.n, v, U.p, U.i, 1, np.array([0, 1], np.int32), np.array([0, U.n], np.int32), bad)
+    assert e.value.status == ERR_BAD_SCHEDULE
+    assert np.array_equal(v, U.x)

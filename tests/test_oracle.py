@@ -164,3 +164,27 @@ def test_pcg_and_gmres_oracles_converge(orc):
     bc = rng.uniform(-1, 1, C.n)
     x, it, rel = orc.gmres_ilu0(C.n, C.astuple(), lu, d, bc, 30, 100, 1e-10)
     assert rel < 1e-9
+
+
+def test_reference_lbc_factorisations_vs_serial_oracle(orc, ref):
+    """The compiled reference's LBC factorisations against the serial oracle:
+    spilu0_csr_lbc's rows do not depend on the schedule, so it equals
+    spilu0_csr bit for bit; spic0_csr_lbc subtracts under `omp atomic`, so
+    its order of updates (and its rounding) can differ run to run: within
+    1e-12 of the serial factor."""
+    from sympiler_gb300 import sym_lib
+    A = mg.convdiff3d(10)
+    d = mg.diag_ptr(A)
+    Lpat = mg.tril(A)
+    nl, lp, pn, pp, nodes = sym_lib.get_coarse_levelSet_DAG_CSC_tree(A.n, Lpat.p, Lpat.i, 0, 4, -1, 100)
+    serial, ok = orc.spilu0_csr(A.n, A.p, A.i, A.x, d)
+    assert ok
+    assert np.array_equal(ref.spilu0_csr_lbc(A.n, A.p, A.i, A.x, d, nl, lp, pp, nodes), serial)
+    S = mg.lap3d(10, 1e-2)
+    U = mg.triu(S)
+    L = mg.transpose(U)
+    nl, lp, pn, pp, nodes = sym_lib.get_coarse_levelSet_DAG_CSC_tree(U.n, L.p, L.i, 0, 4, -1, 100)
+    serial, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+    assert ok
+    lbc = ref.spic0_csr_lbc(U.n, U.p, U.i, U.x, nl, lp, pp, nodes)
+    assert np.allclose(lbc, serial, rtol=1e-12, atol=0)
