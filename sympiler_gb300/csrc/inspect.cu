@@ -27,6 +27,7 @@
 #include <climits>
 #include <cstdlib>
 #include <cstring>
+#include <deque>
 #include <vector>
 
 #include "gbsym.h"
@@ -34,41 +35,39 @@
 namespace gbsym {
 namespace {
 
-// Level set of a forest, leaves first: each sweep over the index window
-// [lo, hi] takes, in ascending index order, every node whose children are
-// all placed; then the window shrinks past finished ends and the placed
-// nodes release their parents.
+// Level set of a forest, leaves first, ascending index within a level.
+// The reference builds it by sweeps over a shrinking index window, each
+// sweep taking in ascending order every node whose children earlier sweeps
+// placed; so a node's level is 0 for a leaf and otherwise one more than its
+// highest child.  With parent[v] > v every child precedes its parent, so
+// one ascending pass finds the levels and a counting sort lists them: O(n)
+// where the sweeps cost O(n * levels), which on the path-shaped
+// elimination tree of a naturally ordered grid is quadratic.
 int forest_levels(int n, const int *parent, int *lptr, int *lset) {
-  std::vector<int> pending(n, 0);
-  std::vector<char> placed(n, 0);
-  for (int v = 0; v < n; ++v)
-    if (parent[v] >= 0) pending[parent[v]]++;
-  int lo = 0, hi = n - 1, nl = 0, cnt = 0;
-  lptr[0] = 0;
-  while (lo <= hi) {
-    for (int v = lo; v <= hi; ++v)
-      if (pending[v] == 0 && !placed[v]) {
-        placed[v] = 1;
-        lset[cnt++] = v;
-      }
-    ++nl;
-    lptr[nl] = cnt;
-    if (cnt == n) break;
-    while (lo < n && pending[lo] == 0) ++lo;
-    while (lo <= hi && pending[hi] == 0) --hi;
-    for (int q = lptr[nl - 1]; q < lptr[nl]; ++q)
-      if (parent[lset[q]] >= 0) pending[parent[lset[q]]]--;
+  std::vector<int> lev(n, 0);
+  int nl = 0;
+  for (int v = 0; v < n; ++v) {
+    nl = std::max(nl, lev[v] + 1);
+    if (parent[v] >= 0) lev[parent[v]] = std::max(lev[parent[v]], lev[v] + 1);
   }
+  std::fill(lptr, lptr + nl + 1, 0);
+  for (int v = 0; v < n; ++v) lptr[lev[v] + 1]++;
+  for (int l = 0; l < nl; ++l) lptr[l + 1] += lptr[l];
+  std::vector<int> fill(lptr, lptr + nl);
+  for (int v = 0; v < n; ++v) lset[fill[lev[v]]++] = v;
   return nl;
 }
 
-int depth_of(int v, const int *parent) {
-  int d = 0;
-  while (parent[v] >= 0) {
-    v = parent[v];
-    ++d;
+// Largest depth (edges to the root) in a forest with parent[v] > v: one
+// descending pass, each node one deeper than its parent.
+int forest_height(int n, const int *parent) {
+  std::vector<int> depth(n, 0);
+  int h = 0;
+  for (int v = n - 1; v >= 0; --v) {
+    if (parent[v] >= 0) depth[v] = depth[parent[v]] + 1;
+    h = std::max(h, depth[v]);
   }
-  return d;
+  return h;
 }
 
 // Children lists of a forest (children in ascending index); nchild must be
@@ -125,7 +124,7 @@ void post_order_pieces(int n, const int *tree, const double *cost, const std::ve
                        const std::vector<int> &cidx, std::vector<int> &nchild, std::vector<double> &piece_cost,
                        std::vector<std::vector<int>> &pieces) {
   std::vector<char> visited(n, 0), mark(n, 0);
-  std::vector<int> work;  // front = index 0
+  std::deque<int> work;  // taken from the front; pushed at either end
   pieces.clear();
   pieces.emplace_back();
   int cur = 0;
@@ -135,7 +134,7 @@ void post_order_pieces(int n, const int *tree, const double *cost, const std::ve
     while (!work.empty()) {
       const int k = work[0];
       if (nchild[k] == 0) {
-        work.erase(work.begin());
+        work.pop_front();
         pieces[cur].push_back(k);
         piece_cost[cur] += cost[k];
         visited[k] = 1;
@@ -143,7 +142,7 @@ void post_order_pieces(int n, const int *tree, const double *cost, const std::ve
         if (p < 0) break;
         nchild[p]--;
         if (!visited[p]) {
-          if (!mark[p]) work.insert(work.begin(), p);
+          if (!mark[p]) work.push_front(p);
           mark[p] = 1;
         }
       } else {
@@ -165,7 +164,7 @@ void post_order_pieces(int n, const int *tree, const double *cost, const std::ve
             visited[c] = 1;
             nchild[tree[c]]--;
           } else {
-            work.insert(work.begin(), c);
+            work.push_front(c);
           }
         }
       }
@@ -211,9 +210,7 @@ int tree_lbc(int n, const int *parent, const double *cost, int inner_parts, int 
   std::vector<int> nchild(n, 0);
   for (int v = 0; v < n; ++v)
     if (parent[v] >= 0) nchild[parent[v]]++;
-  int height = 0;
-  for (int v = 0; v < n; ++v)
-    if (nchild[v] == 0) height = std::max(height, depth_of(v, parent));
+  const int height = forest_height(n, parent);
   if (height == 0 && n == 1) {
     level_ptr[1] = 1;
     part_ptr[1] = 1;
