@@ -199,24 +199,38 @@ def _banded_lower(n, w, seed):
     return mg.from_scipy(sp.diags(diags, offs, shape=(n, n), format="csr"))
 
 
+def _banded_with_long_rows(n, w, seed):
+    """_banded_lower plus three rows holding ~n/7 off-diagonals each: the
+    slab stays w wide and those rows run the overflow path."""
+    import scipy.sparse as sp
+    B = _banded_lower(n, w, seed).scipy().tolil()
+    rng = np.random.default_rng(seed + 1)
+    for i in (n // 2, n - 3, n - 1):
+        for j in range(0, i - w, 7):
+            B[i, j] = rng.uniform(-1.0, 1.0) / n
+    return mg.from_scipy(B.tocsr())
+
+
 @pytest.mark.parametrize("w", [1, 2, 3, 4, 5, 8])
 def test_syncfree_every_slab_width(gpu, orc, w):
     """The sync-free sweep is compiled once per slab width (2, 3, 4 and the
     full 8); each width's kernels match the oracle bit for bit in FP64 at 1,
-    8 and 64 right-hand sides and in FP32 at one."""
+    8 and 64 right-hand sides, with and without rows past the slab (the
+    overflow path), and in FP32 at one."""
     from sympiler_gb300._lib import EXEC_SYNCFREE
     from sympiler_gb300.plans import TriPlan
-    L = _banded_lower(4099, w, seed=w)
-    plan = TriPlan(L.n, *L.astuple())
-    plan.set_exec(EXEC_SYNCFREE)
     rng = np.random.default_rng(100 + w)
-    for k in (1, 8, 64):
-        B = rng.standard_normal((L.n, k))
-        ref = _oracle_mrhs(orc, L, B)
-        x = torch.from_numpy(B.copy()).cuda()
-        plan.solve(x if k > 1 else x.view(-1))
-        plan.check()
-        assert np.array_equal(x.cpu().numpy(), ref), (w, k)
+    for L in (_banded_lower(4099, w, seed=w), _banded_with_long_rows(4099, w, seed=w)):
+        plan = TriPlan(L.n, *L.astuple())
+        plan.set_exec(EXEC_SYNCFREE)
+        for k in (1, 8, 64):
+            B = rng.standard_normal((L.n, k))
+            ref = _oracle_mrhs(orc, L, B)
+            x = torch.from_numpy(B.copy()).cuda()
+            plan.solve(x if k > 1 else x.view(-1))
+            plan.check()
+            assert np.array_equal(x.cpu().numpy(), ref), (w, k)
+    L = _banded_lower(4099, w, seed=w)
     p32 = TriPlan(L.n, *L.astuple(), dtype="f32")
     p32.set_exec(EXEC_SYNCFREE)
     b32 = rng.standard_normal(L.n).astype(np.float32)
