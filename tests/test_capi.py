@@ -69,6 +69,9 @@ int main(int argc, char **argv) {
     sym_lib::spmv_csr(n, p, i, v, x, y, z, 1.0, 0.0);
     sym_lib::ltsolve(n, p, i, v, x);
     sym_lib::spic0_csr(n, v, p, i);
+    sym_lib::spic0_csr_lbc(n, v, p, i, 1, p, p, i);
+    sym_lib::spilu0_csr(n, 1, p, i, v, i, y);
+    sym_lib::spilu0_csr_lbc(n, 1, p, i, v, i, y, 1, p, p, i, nullptr);
     sym_lib::parsy::lsolve(n, p, i, v, x);
     sym_lib::parsy::lus_cr(n, 1, p, i, v, i, x, y);
     size_t zp[2] = {0, 1};
