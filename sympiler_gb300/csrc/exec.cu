@@ -118,11 +118,14 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   const long long m = (long long)t->n * k;
   DBuf<T> buf(m);
   // (executor, parameter) candidates: the sync-free sweep is tried at one,
-  // two and three blocks per SM, the partitioned executor (k = 1 only) at
-  // several partition sizes
+  // two and three blocks per SM (parameter bits 0-2) and, for several FP64
+  // right-hand sides, with lanes of one or two values per row (bit 3); the
+  // partitioned executor (k = 1 only) at several partition sizes
   std::vector<std::pair<int, int>> cands = {{GBSYM_EXEC_LEVELSET, 0}, {GBSYM_EXEC_PERSISTENT, 0},
                                             {GBSYM_EXEC_SYNCFREE, 1}, {GBSYM_EXEC_SYNCFREE, 2},
                                             {GBSYM_EXEC_SYNCFREE, 3}, {GBSYM_EXEC_CLUSTER, 0}};
+  if (k > 1 && sizeof(T) == 8)
+    for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | 8});
   if (k == 1 && t->max_level_rows <= 4096) cands.push_back({GBSYM_EXEC_ONEBLOCK, 0});
   if (k == 1) {
     std::vector<int> sizes;
@@ -145,11 +148,14 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   float best_ms = 0;
   const int saved_rows = t->part_rows_pref;
   const int kk = k > 1 ? 1 : 0;
-  const int saved_bps = t->sf_bps_tuned[kk];
+  const int saved_bps = t->sf_bps_tuned[kk], saved_pair = t->sf_pair_lanes;
   for (const auto &cand : cands) {
     const int e = cand.first;
     if (e == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = cand.second;
-    if (e == GBSYM_EXEC_SYNCFREE) t->sf_bps_tuned[kk] = cand.second;
+    if (e == GBSYM_EXEC_SYNCFREE) {
+      t->sf_bps_tuned[kk] = cand.second & 7;
+      if (k > 1) t->sf_pair_lanes = cand.second >> 3;
+    }
     std::vector<float> ms;
     for (int rep = 0; rep < 4; ++rep) {
       k_fill_tune<T><<<(int)std::min<long long>(div_up(m, 256), num_sms() * 8), 256, 0, s>>>(buf.p, m);
@@ -176,9 +182,13 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   cudaEventDestroy(e1);
   t->part_rows_pref = saved_rows;
   t->sf_bps_tuned[kk] = saved_bps;
+  t->sf_pair_lanes = saved_pair;
   if (best < 0) throw Err{GBSYM_ERR_TIMEOUT};
   if (best == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = best_rows;
-  if (best == GBSYM_EXEC_SYNCFREE) t->sf_bps_tuned[kk] = best_rows;
+  if (best == GBSYM_EXEC_SYNCFREE) {
+    t->sf_bps_tuned[kk] = best_rows & 7;
+    if (k > 1) t->sf_pair_lanes = best_rows >> 3;
+  }
   if (k == 1) t->exec = best; else t->exec_mrhs = best;
   std::lock_guard<std::mutex> lk(g_tuned_mu);
   g_tuned[tune_key(t, k, dtype)] = best;

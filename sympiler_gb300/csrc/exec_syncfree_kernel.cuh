@@ -299,13 +299,16 @@ static void sf_ar(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
     sf_gk<T, 4, AR, KS>(t, x, y, k, s);
     return;
   }
-  // FP64 lanes carry one value each, so a row takes the next power of two
-  // at or above k lanes (at most 32): one slice per row up to 32
-  // right-hand sides (C2: 8 RHS 260 -> 246 us, 32 RHS 325 -> 308 us against
-  // lanes sized for two values each); FP32 lanes carry two or four.
+  // FP64 lanes carry one value each, so by default a row takes the next
+  // power of two at or above k lanes (at most 32): one slice per row up to
+  // 32 right-hand sides (C2: 8 RHS 260 -> 246 us, 32 RHS 325 -> 308 us
+  // against half as many lanes, each taking two slices).  Which is faster
+  // depends on the matrix (the C4 batch prefers half at 8 RHS), so the
+  // autotuner chooses (sf_pair_lanes).  FP32 lanes carry two or four.
   int g64 = 2;
   while (g64 < k && g64 < 32) g64 <<= 1;
-  switch (sizeof(T) == 8 ? g64 : lanes_for(k, sizeof(T))) {
+  const bool pair = t->sf_pair_lanes == 1;
+  switch (sizeof(T) == 8 && !pair ? g64 : lanes_for(k, sizeof(T))) {
     case 2: sf_gk<T, 2, AR, KS>(t, x, y, k, s); break;
     case 4: sf_gk<T, 4, AR, KS>(t, x, y, k, s); break;
     case 8: sf_gk<T, 8, AR, KS>(t, x, y, k, s); break;
