@@ -135,3 +135,27 @@ def test_inspectors_reject_bad_input():
         sym_lib.parsy.getCoarseLevelSet_6(2, np.array([1, -1], np.int32), None, 0, -1, 4000, np.ones(2))
     assert sym_lib.get_coarse_levelSet_DAG_CSC_tree(0, np.zeros(1, np.int32), np.zeros(0, np.int32),
                                                     0, 4, -1, 4000)[0] == 0
+
+
+def test_inspectors_are_linear_on_path_shaped_trees():
+    """A naturally ordered grid's elimination tree is a single path, so the
+    level set has as many levels as nodes.  The reference's per-level window
+    sweep is quadratic there; the inspectors must stay linear: a 300,000-node
+    path and the DAG LBC of the 48^3 grid's factor each take well under a
+    second, with the level set one node per level."""
+    import time
+    n = 300_000
+    parent = np.arange(1, n + 1, dtype=np.int32)
+    parent[-1] = -1
+    lp, ls = np.zeros(n + 1, np.int32), np.zeros(n, np.int32)
+    t0 = time.perf_counter()
+    nl = sym_lib.parsy.getLevelSet(n, parent, lp, ls)
+    cost = np.ones(n)
+    lvl = sym_lib.parsy.getCoarseLevelSet_6(n, parent, None, 64, -1, 4000, cost)
+    assert time.perf_counter() - t0 < 2.0
+    assert nl == n and np.array_equal(ls, np.arange(n)) and np.array_equal(lp, np.arange(n + 1))
+    assert lvl[2] >= 1 and np.array_equal(np.sort(lvl[4]), np.arange(n))
+    L = mg.tril(mg.lap3d(48, 1e-2))
+    t0 = time.perf_counter()
+    sym_lib.get_coarse_levelSet_DAG_CSC_tree(L.n, L.p, L.i, 0, 64, -1, 4000)
+    assert time.perf_counter() - t0 < 2.0
