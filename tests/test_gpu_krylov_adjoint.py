@@ -68,7 +68,11 @@ def _dense_grad(L, X, W):
     return GB, G[rows, L.i]
 
 
-def test_adjoint_dense_and_finite_differences(gpu, orc):
+@pytest.mark.parametrize("k", [6, 8, 32])
+def test_adjoint_dense_and_finite_differences(gpu, orc, k):
+    """The reverse pass against a dense FP64 reference and central finite
+    differences; k = 8 and 32 take the four-lanes-per-row value gradient,
+    k = 6 the one-thread-per-row one."""
     from sympiler_gb300._lib import UPPER_DIAG_FIRST
     from sympiler_gb300.plans import TriPlan, tri_adjoint
     rng = np.random.default_rng(5)
@@ -77,7 +81,6 @@ def test_adjoint_dense_and_finite_differences(gpu, orc):
     f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
     Lt = mg.CSR(U.n, U.p, U.i, f)
     L = mg.transpose(Lt)
-    k = 6
     B = rng.standard_normal((L.n, k))
     W = rng.standard_normal((L.n, k))
     P = TriPlan(L.n, *L.astuple())
