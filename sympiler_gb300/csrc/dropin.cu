@@ -500,11 +500,8 @@ static void ic0_dropin(int n, double *val, const int *rowPtr, const int *colIdx,
   GB_CHECK(n >= 0, GBSYM_ERR_SIZE);
   if (n == 0) return;
   GB_CHECK(val && rowPtr && colIdx, GBSYM_ERR_NULL_ARG);
-  cudaStream_t s = thread_stream();
   const int nnz = rowPtr[n];
   GB_CHECK(nnz >= 0, GBSYM_ERR_BAD_MATRIX);
-  DBuf<int> dp, di;
-  DBuf<double> dv;
   if (lbc) {
     // structure first, on the host, before any kernel indexes with it
     GB_CHECK(rowPtr[0] == 0, GBSYM_ERR_BAD_MATRIX);
@@ -514,6 +511,9 @@ static void ic0_dropin(int n, double *val, const int *rowPtr, const int *colIdx,
         GB_CHECK(colIdx[e] > r && colIdx[e] < n, GBSYM_ERR_BAD_MATRIX);
     }
   }
+  cudaStream_t s = thread_stream();
+  DBuf<int> dp, di;
+  DBuf<double> dv;
   upload(dp, rowPtr, n + 1, false, s);
   upload(di, colIdx, nnz, false, s);
   upload(dv, val, nnz, false, s);

@@ -145,3 +145,29 @@ int main() {
     par = sym_lib.etree_lower_csr(L.n, L.p, L.i)
     tlp, tls = np.zeros(L.n + 1, np.int32), np.zeros(L.n, np.int32)
     assert int(lines[4]) == sym_lib.parsy.getLevelSet(L.n, par, tlp, tls)
+
+
+def test_lbc_factor_drop_ins_check_arguments_on_the_host():
+    """spilu0_csr_lbc / spic0_csr_lbc report argument errors before any
+    device work, so these run without a GPU: n = 0 is a no-op, null arrays
+    give NULL_ARG, and an upper CSR whose row does not start with its
+    diagonal gives BAD_MATRIX under an LBC schedule."""
+    import ctypes as C
+    from sympiler_gb300 import _lib
+    L = _lib.lib()
+    P = lambda a: a.ctypes.data_as(C.c_void_p)  # noqa: E731
+    L.gbsym_spilu0_csr_lbc(0, 0, None, None, None, None, None, 0, None, None, None, None)
+    assert L.gbsym_last_error() == _lib.OK
+    L.gbsym_spic0_csr_lbc(0, None, None, None, 0, None, None, None)
+    assert L.gbsym_last_error() == _lib.OK
+    L.gbsym_spilu0_csr_lbc(3, 3, None, None, None, None, None, 1, None, None, None, None)
+    assert L.gbsym_last_error() == _lib.ERR_NULL_ARG
+    L.gbsym_spic0_csr_lbc(3, None, None, None, 1, None, None, None)
+    assert L.gbsym_last_error() == _lib.ERR_NULL_ARG
+    rp = np.array([0, 2, 3, 4], np.int32)
+    ci = np.array([0, 2, 2, 2], np.int32)  # row 1 starts with column 2, not its diagonal
+    v = np.ones(4)
+    lp, pp, part = np.array([0, 1], np.int32), np.array([0, 3], np.int32), np.arange(3, dtype=np.int32)
+    L.gbsym_spic0_csr_lbc(3, P(v), P(rp), P(ci), 1, P(lp), P(pp), P(part))
+    assert L.gbsym_last_error() == _lib.ERR_BAD_MATRIX
+    assert np.all(v == 1.0)
