@@ -7,6 +7,7 @@ import re
 import subprocess
 
 import numpy as np
+import pytest
 
 from conftest import ROOT
 
@@ -171,3 +172,33 @@ def test_lbc_factor_drop_ins_check_arguments_on_the_host():
     L.gbsym_spic0_csr_lbc(3, P(v), P(rp), P(ci), 1, P(lp), P(pp), P(part))
     assert L.gbsym_last_error() == _lib.ERR_BAD_MATRIX
     assert np.all(v == 1.0)
+
+
+@pytest.mark.parametrize("name,nint", [("gbsym_sptrsv_csr", 0), ("gbsym_sptrsv_csc", 0), ("gbsym_spmv_csr", 0),
+                                       ("gbsym_spilu0_csr", 1), ("gbsym_parsy_lus_cr", 1),
+                                       ("gbsym_sptrsv_csr_levelset", 0)])
+def test_drop_ins_report_null_arrays_without_a_gpu(name, nint):
+    """The void drop-ins record NULL_ARG for null arrays, and n = 0 is a
+    no-op, before any device work (so these run without a GPU); the int
+    forms also return 0."""
+    from sympiler_gb300 import _lib
+    L = _lib.lib()
+    f = getattr(L, name)
+    argtypes = _lib.SIGNATURES[name][1]
+    def args(n):
+        out = [n]
+        ints_left = nint
+        for t in argtypes[1:]:
+            if t is _lib.C.c_int:
+                out.append(n if ints_left else 1)
+                ints_left = max(0, ints_left - 1)
+            else:
+                out.append(None)
+        return out
+    f(*args(0))
+    assert L.gbsym_last_error() == _lib.OK
+    f(*args(4))
+    assert L.gbsym_last_error() == _lib.ERR_NULL_ARG
+    for fn in (L.gbsym_ltsolve, L.gbsym_parsy_lsolve):
+        assert fn(4, None, None, None, None) == 0
+        assert L.gbsym_last_error() == _lib.ERR_NULL_ARG
