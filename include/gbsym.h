@@ -526,12 +526,28 @@ typedef struct gbsym_batch_s *gbsym_batch;
 int gbsym_batch_create(gbsym_batch *out, int nsys, const int *n,
                        const int *const *Lp, const int *const *Li,
                        const double *const *Lx, int value_dtype, void *stream);
+/* The same with the triangles' storage named: GBSYM_LOWER_DIAG_LAST (as
+ * gbsym_batch_create) or GBSYM_LOWER_CSC (lower CSC, diagonal first: the
+ * upper CSR an IC0 factor is computed in, as spic0_csr leaves it).  Every
+ * column index must lie inside its own system (GBSYM_ERR_BAD_MATRIX
+ * otherwise). */
+int gbsym_batch_create_kind(gbsym_batch *out, int nsys, const int *n,
+                            const int *const *Lp, const int *const *Li,
+                            const double *const *Lx, int kind, int value_dtype,
+                            void *stream);
 int gbsym_batch_destroy(gbsym_batch b);
 /* x: device, concatenation of the systems' row-major n_s x k blocks (FP64
  * or FP32).  offsets (host, nsys+1) receives the row offset of each system
  * when non-NULL. */
 int gbsym_batch_solve(gbsym_batch b, void *x, int k, int dtype, void *stream);
 int gbsym_batch_row_offsets(gbsym_batch b, long long *offsets);
+/* Executor choice for k right-hand sides, timed on the batch itself (as
+ * gbsym_tri_autotune on the pooled triangle). */
+int gbsym_batch_autotune(gbsym_batch b, int k, int dtype, void *stream, int *chosen);
+/* Synchronises `stream`; returns a status a bounded device wait recorded. */
+int gbsym_batch_check(gbsym_batch b, void *stream);
+/* Size, levels and storage of the pooled triangle. */
+int gbsym_batch_get_info(gbsym_batch b, gbsym_tri_info *info);
 
 /* ---- forward solve that allocates nothing ------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device
@@ -542,10 +558,14 @@ int gbsym_batch_row_offsets(gbsym_batch b, long long *offsets);
  * reference sptrsv_csr arithmetic (bit-identical results).  Its only scratch
  * is a static device array inside this library (4 MiB per GPU, held until
  * the process exits), so n is limited to 524,288 rows; larger n returns
- * GBSYM_ERR_SIZE without touching x.  The first call on a device looks up
- * that array's address and should come before any stream capture; calls
- * that overlap on the GPU share the array and race.  Returns when the
- * solve is done (synchronises `stream`). */
+ * GBSYM_ERR_SIZE without touching x.  The first call on a device does that
+ * device's set-up (it looks up the array's address) and should come before
+ * any stream capture; calls that overlap on the GPU share the array and
+ * race.  Returns when the solve is done (it synchronises `stream`).
+ * Precondition: Lp[0..n] is non-decreasing and Lp[n] lies within Li and
+ * Lx -- the kernel reads Li[Lp[i] .. Lp[i+1]) unchecked.  Column indices
+ * are checked: one outside [0, i) in row i returns GBSYM_ERR_BAD_MATRIX.
+ * After GBSYM_ERR_BAD_MATRIX or GBSYM_ERR_TIMEOUT, x is undefined. */
 int gbsym_sptrsv_csr_noalloc(int n, const int *Lp, const int *Li, const double *Lx, double *x,
                              void *stream);
 

@@ -114,6 +114,10 @@ SIGNATURES = {
     "gbsym_batch_destroy": (_int, [_vp]),
     "gbsym_batch_solve": (_int, [_vp, _vp, _int, _int, _vp]),
     "gbsym_batch_row_offsets": (_int, [_vp, _vp]),
+    "gbsym_batch_create_kind": (_int, [C.POINTER(_vp), _int, _vp, _vp, _vp, _vp, _int, _int, _vp]),
+    "gbsym_batch_autotune": (_int, [_vp, _int, _int, _vp, _pi]),
+    "gbsym_batch_check": (_int, [_vp, _vp]),
+    "gbsym_batch_get_info": (_int, [_vp, C.POINTER(TriInfo)]),
     "gbsym_sptrsv_csr_noalloc": (_int, [_int, _vp, _vp, _vp, _vp, _vp]),
 }
 

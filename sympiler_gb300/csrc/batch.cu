@@ -24,11 +24,19 @@ struct gbsym_batch_s {
 
 using namespace gbsym;
 
-extern "C" int gbsym_batch_create(gbsym_batch *out, int nsys, const int *n, const int *const *Lp,
-                                  const int *const *Li, const double *const *Lx, int value_dtype,
-                                  void *stream) {
+// Packs the systems into one block-diagonal pool on the device.  kind is
+// GBSYM_LOWER_DIAG_LAST (lower CSR, diagonal last in each row) or
+// GBSYM_LOWER_CSC (lower CSC, diagonal first in each column: the upper CSR
+// an IC0 factor is computed in), which the pool plan transposes on the
+// device as gbsym_tri_create does for one system.  Every column index is
+// checked against its own system's size on the host while packing, so no
+// entry can reach into another system.
+static int batch_create(gbsym_batch *out, int nsys, const int *n, const int *const *Lp,
+                        const int *const *Li, const double *const *Lx, int kind, int value_dtype,
+                        void *stream) {
   if (!out || nsys < 0 || (nsys > 0 && (!n || !Lp || !Li || !Lx))) return GBSYM_ERR_NULL_ARG;
   *out = nullptr;
+  if (kind != GBSYM_LOWER_DIAG_LAST && kind != GBSYM_LOWER_CSC) return GBSYM_ERR_UNSUPPORTED;
   return guarded([&] {
     cudaStream_t s = (cudaStream_t)stream;
     std::unique_ptr<gbsym_batch_s> b(new gbsym_batch_s());
@@ -38,7 +46,10 @@ extern "C" int gbsym_batch_create(gbsym_batch *out, int nsys, const int *n, cons
     for (int q = 0; q < nsys; ++q) {
       GB_CHECK(n[q] >= 0 && (n[q] == 0 || (Lp[q] && Li[q] && Lx[q])), GBSYM_ERR_NULL_ARG);
       b->off[q + 1] = b->off[q] + n[q];
-      nnz += n[q] ? Lp[q][n[q]] : 0;
+      if (n[q]) {
+        GB_CHECK(Lp[q][0] == 0 && Lp[q][n[q]] >= 0, GBSYM_ERR_BAD_MATRIX);
+        nnz += Lp[q][n[q]];
+      }
     }
     GB_CHECK(b->off[nsys] < (1ll << 31) && nnz < (1ll << 31), GBSYM_ERR_SIZE);
     const int N = (int)b->off[nsys];
@@ -48,15 +59,16 @@ extern "C" int gbsym_batch_create(gbsym_batch *out, int nsys, const int *n, cons
     for (int q = 0; q < nsys; ++q) {
       const int rows = n[q];
       const int base = (int)b->off[q];
-      const int e0 = rows ? Lp[q][0] : 0;
       for (int r = 0; r < rows; ++r) {
         P[base + r] = (int)e;
+        GB_CHECK(Lp[q][r] <= Lp[q][r + 1], GBSYM_ERR_BAD_MATRIX);
         for (int t = Lp[q][r]; t < Lp[q][r + 1]; ++t, ++e) {
-          I[e] = Li[q][t] + base;
+          const int c = Li[q][t];
+          GB_CHECK(c >= 0 && c < rows, GBSYM_ERR_BAD_MATRIX);
+          I[e] = c + base;
           X[e] = Lx[q][t];
         }
       }
-      (void)e0;
     }
     P[N] = (int)e;
     DBuf<int> dp, di;
@@ -64,10 +76,26 @@ extern "C" int gbsym_batch_create(gbsym_batch *out, int nsys, const int *n, cons
     upload(dp, P.data(), N + 1, false, s);
     upload(di, I.data(), e, false, s);
     upload(dx, X.data(), e, false, s);
-    b->pool.reset(tri_build(N, dp.p, di.p, dx.p, nullptr, GBSYM_LOWER_DIAG_LAST, value_dtype, nullptr,
-                            nullptr, 0, s));
+    gbsym_tri pool = nullptr;
+    const int st = gbsym_tri_create(&pool, N, dp.p, di.p, dx.p, nullptr, kind, value_dtype, 1, nullptr,
+                                    nullptr, 0, s);
+    if (st != GBSYM_OK) throw Err{st};
+    b->pool.reset(pool);
+    GB_CUDA(cudaStreamSynchronize(s));  // the packed plan no longer needs the staging copies
     *out = b.release();
   });
+}
+
+extern "C" int gbsym_batch_create(gbsym_batch *out, int nsys, const int *n, const int *const *Lp,
+                                  const int *const *Li, const double *const *Lx, int value_dtype,
+                                  void *stream) {
+  return batch_create(out, nsys, n, Lp, Li, Lx, GBSYM_LOWER_DIAG_LAST, value_dtype, stream);
+}
+
+extern "C" int gbsym_batch_create_kind(gbsym_batch *out, int nsys, const int *n, const int *const *Lp,
+                                       const int *const *Li, const double *const *Lx, int kind,
+                                       int value_dtype, void *stream) {
+  return batch_create(out, nsys, n, Lp, Li, Lx, kind, value_dtype, stream);
 }
 
 extern "C" int gbsym_batch_destroy(gbsym_batch b) {
@@ -82,6 +110,21 @@ extern "C" int gbsym_batch_solve(gbsym_batch b, void *x, int k, int dtype, void 
     tri_solve_rowmajor(b->pool.get(), x, nullptr, k, dtype,
                        (cudaStream_t)stream);
   });
+}
+
+extern "C" int gbsym_batch_autotune(gbsym_batch b, int k, int dtype, void *stream, int *chosen) {
+  if (!b) return GBSYM_ERR_NULL_ARG;
+  return gbsym_tri_autotune(b->pool.get(), k, dtype, stream, chosen);
+}
+
+extern "C" int gbsym_batch_check(gbsym_batch b, void *stream) {
+  if (!b) return GBSYM_ERR_NULL_ARG;
+  return gbsym_tri_check(b->pool.get(), stream);
+}
+
+extern "C" int gbsym_batch_get_info(gbsym_batch b, gbsym_tri_info *info) {
+  if (!b) return GBSYM_ERR_NULL_ARG;
+  return gbsym_tri_get_info(b->pool.get(), info);
 }
 
 extern "C" int gbsym_batch_row_offsets(gbsym_batch b, long long *offsets) {

@@ -36,14 +36,19 @@ cudaStream_t thread_stream() {
   return pt.streams[dev];
 }
 
+// SM count of the current device, cached per device.  The entries are
+// atomics: any host thread may fill one (they all store the same value).
 int num_sms() {
-  static int cache[64] = {0};
+  static std::atomic<int> cache[64];
   int dev = 0;
   GB_CUDA(cudaGetDevice(&dev));
-  if (dev < 64 && cache[dev]) return cache[dev];
+  if (dev < 64) {
+    const int c = cache[dev].load(std::memory_order_relaxed);
+    if (c) return c;
+  }
   int v = 0;
   GB_CUDA(cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev));
-  if (dev < 64) cache[dev] = v;
+  if (dev < 64) cache[dev].store(v, std::memory_order_relaxed);
   return v;
 }
 

@@ -25,12 +25,22 @@
 // Waits are bounded; a malformed row (a column outside [0, row)) is
 // reported, not followed.
 //
-// The first call on a device looks up the device address of the static
-// array (cudaGetSymbolAddress, with that device current) and remembers it;
-// make that first call before any stream capture.  Every call shares the
-// array and leaves the last call's contents in it, so calls that overlap
-// on the GPU (different streams, or different host threads on one device)
-// race: serialise them.
+// The first call on a device does that device's set-up: it looks up the
+// device address of the static array (cudaGetSymbolAddress, with that
+// device current) and the kernel's resident blocks per SM, and remembers
+// both; make that first call before any stream capture.  Every call
+// clears the part of the array it uses, runs the sweep and copies the
+// error word back, and returns only after the solve has finished on its
+// stream.  All calls share the array and the last call's contents stay in
+// it, so calls that overlap on the GPU (different streams, or different
+// host threads on one device) race: serialise them.
+//
+// The caller's row pointers must be valid: Lp[0..n] non-decreasing and
+// every Lp[i+1] within Li and Lx, since the kernel reads
+// Li[Lp[i] .. Lp[i+1]) without knowing the arrays' lengths.  Column
+// indices are checked before use.  After GBSYM_ERR_BAD_MATRIX or
+// GBSYM_ERR_TIMEOUT the contents of x are undefined (rows finished before
+// the error keep their solved values).
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -50,6 +60,7 @@ static __device__ __align__(256) unsigned long long g_noalloc_scratch[kNoAllocMa
 
 struct DeviceScratch {
   unsigned long long *ptr = nullptr;  // device address of g_noalloc_scratch
+  int per_sm = 0;                     // resident blocks of the sweep per SM
   bool ready = false;
 };
 static std::mutex g_na_mu;
@@ -130,9 +141,10 @@ k_noalloc_forward(int n, const int *__restrict__ Lp, const int *__restrict__ Li,
   }
 }
 
-// Device address of the static array for the current device, looked up
-// once per device (with that device current) and remembered.
-static unsigned long long *scratch_for_current_device() {
+// Device address of the static array for the current device and the
+// sweep's resident blocks per SM, looked up once per device (with that
+// device current) and remembered.
+static DeviceScratch scratch_for_current_device() {
   int dev = 0;
   GB_CUDA(cudaGetDevice(&dev));
   GB_CHECK(dev >= 0 && dev < 64, GBSYM_ERR_UNSUPPORTED);
@@ -145,10 +157,13 @@ static unsigned long long *scratch_for_current_device() {
       std::fprintf(stderr, "gbsym: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
       throw Err{GBSYM_ERR_CUDA};
     }
+    int per_sm = 0;
+    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_noalloc_forward, kNaBlock, 0));
     d.ptr = static_cast<unsigned long long *>(p);
+    d.per_sm = per_sm;
     d.ready = true;
   }
-  return d.ptr;
+  return d;
 }
 
 }  // namespace
@@ -167,13 +182,14 @@ extern "C" int gbsym_sptrsv_csr_noalloc(int n, const int *Lp, const int *Li, con
   int code = GBSYM_OK;
   const int st = guarded([&] {
     cudaStream_t s = (cudaStream_t)stream;
-    unsigned long long *scratch = scratch_for_current_device();
+    const DeviceScratch d = scratch_for_current_device();
+    // the cooperative sweep needs one resident block on every SM
+    GB_CHECK(d.per_sm >= 1, GBSYM_ERR_UNSUPPORTED);
+    unsigned long long *scratch = d.ptr;
     // published values start as the sentinel; the error word starts at zero
     GB_CUDA(cudaMemsetAsync(scratch, 0xff, (size_t)n * sizeof(unsigned long long), s));
     GB_CUDA(cudaMemsetAsync(scratch + kNoAllocMaxRows, 0, sizeof(int), s));
-    int per_sm = 0;
-    GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_noalloc_forward, kNaBlock, 0));
-    const int grid = std::max(1, std::min(per_sm, 1)) * num_sms();
+    const int grid = num_sms();
     void *params[] = {(void *)&n, (void *)&Lp, (void *)&Li, (void *)&Lx, (void *)&x, (void *)&scratch};
     GB_CUDA(cudaLaunchCooperativeKernel((const void *)k_noalloc_forward, dim3(grid), dim3(kNaBlock), params,
                                         0, s));

@@ -315,9 +315,12 @@ def tri_adjoint(Lt: TriPlan, n, Lp, Li, X, g, grad, stream=None):
 
 
 class BatchPlan:
-    """Many lower-triangular CSR systems (diagonal last) solved together."""
+    """Many triangular systems of uneven sizes solved together: lower CSRs
+    with the diagonal last (kind LOWER_DIAG_LAST, the default) or lower CSCs
+    with the diagonal first (kind LOWER_CSC), given as (n, p, i, x) host
+    arrays."""
 
-    def __init__(self, systems, dtype="f64", stream=None):
+    def __init__(self, systems, dtype="f64", kind=L.LOWER_DIAG_LAST, stream=None):
         nsys = len(systems)
         self._keep = []
         ns = (C.c_int * nsys)()
@@ -334,14 +337,32 @@ class BatchPlan:
             is_[q] = i.ctypes.data
             xs[q] = x.ctypes.data
         h = C.c_void_p()
-        check(lib().gbsym_batch_create(C.byref(h), nsys, ns, ps, is_, xs, _dtype_code(dtype),
-                                       _stream(stream)), "gbsym_batch_create")
+        check(lib().gbsym_batch_create_kind(C.byref(h), nsys, ns, ps, is_, xs, int(kind), _dtype_code(dtype),
+                                            _stream(stream)), "gbsym_batch_create_kind")
         self._h = h
         self._keep = None
         self.nsys = nsys
+        self.dtype = _dtype_code(dtype)
         off = np.zeros(nsys + 1, dtype=np.int64)
         check(lib().gbsym_batch_row_offsets(h, off.ctypes.data_as(C.c_void_p)), "gbsym_batch_row_offsets")
         self.offsets = off
+
+    def info(self) -> TriInfo:
+        inf = TriInfo()
+        check(lib().gbsym_batch_get_info(self._h, C.byref(inf)), "gbsym_batch_get_info")
+        return inf
+
+    def autotune(self, k=1, dtype=None, stream=None) -> int:
+        """Time the executors on the batch for k right-hand sides; returns the chosen one."""
+        chosen = C.c_int(0)
+        dt = self.dtype if dtype is None else _dtype_code(dtype)
+        check(lib().gbsym_batch_autotune(self._h, int(k), dt, _stream(stream), C.byref(chosen)),
+              "gbsym_batch_autotune")
+        return chosen.value
+
+    def check(self, stream=None):
+        """Wait for the stream; raise if a bounded device wait gave up."""
+        check(lib().gbsym_batch_check(self._h, _stream(stream)), "gbsym_batch_check")
 
     def solve(self, x, stream=None):
         k = 1 if x.dim() == 1 else x.shape[1]
