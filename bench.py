@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--extras-only", action="store_true")
     ap.add_argument("--supernodal-grid", type=int, default=0,
                     help="run only the supernodal-solve extra, on a G^3 grid's factor (profiling runs)")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4"],
+                    help="c2: one IC0 forward solve with --rhs right-hand sides (default); c4: the 512-system "
+                         "batch, sharded over the ranks")
+    ap.add_argument("--dtype", default="f64", choices=["f64", "f32"], help="c4 workload: factor and vectors")
     ap.add_argument("--exec", default="auto",
                     choices=["auto", "levelset", "syncfree", "oneblock", "persistent", "cluster", "partitioned"],
                     help="force one executor instead of autotuning (profiling runs)")
@@ -150,9 +154,67 @@ def dist_init():
     return world, rank, local
 
 
+def run_reference_c4(args):
+    """The reference arm of the batched workload: every system's forward
+    solve with the oracle's serial sptrsv_csr per right-hand side (the
+    reference executor's arithmetic), systems spread over all host threads."""
+    import oracle
+    from concurrent.futures import ThreadPoolExecutor
+    from sympiler_gb300 import matgen as mg
+    orc = oracle.orc()
+    k, dt = 8, args.dtype
+    systems = mg.batch_systems_upper(512, np.random.default_rng(44))
+    Ls = []
+    for n, p, i, x in systems:
+        f, ok = orc.spic0_csr(n, p, i, x)
+        Ls.append(mg.transpose(mg.CSR(n, p, i, f)))
+    N = sum(L.n for L in Ls)
+    nnz = sum(L.nnz for L in Ls)
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(45)
+    Bs = [rng.standard_normal((k, L.n)) for L in Ls]
+    if dt == "f32":
+        Bs = [B.astype(np.float32) for B in Bs]
+        L32 = [L.x.astype(np.float32) for L in Ls]
+    pool = ThreadPoolExecutor(max_workers=cores)
+
+    def one(q):
+        L, X = Ls[q], Bs[q].copy()
+        if dt == "f64":
+            orc.sptrsv_csr_mrhs(L.n, *L.astuple(), X, k, 1)
+        else:
+            for c in range(k):
+                orc.sptrsv_csr_f32(L.n, L.p, L.i, L32[q], X[c])
+        return X
+
+    order = sorted(range(len(Ls)), key=lambda q: -Ls[q].nnz)  # largest first
+    for _ in range(max(1, min(args.warmup, 2))):
+        list(pool.map(one, order))
+    ts = []
+    for _ in range(max(1, min(args.steps, 5))):
+        t0 = time.perf_counter()
+        list(pool.map(one, order))
+        ts.append(time.perf_counter() - t0)
+    t = statistics.median(ts)
+    vb = 8 if dt == "f64" else 4
+    value = algorithmic_bytes(nnz, N, k, vb, vb) / t / 1e9
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "strong", "vs_baseline": None, "dtype": dt, "data": "synthetic",
+            "config": c4_config(dt, k, 512, 1),
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "cpu": host_cpu(), "kind": "port",
+                             "sample": "all 512 systems x %d RHS per step, serial solves spread over %d host "
+                                       "threads; median of %d" % (k, cores, len(ts))},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args):
     world, rank, _ = dist_init()
     if rank != 0:
+        return
+    if args.workload == "c4":
+        run_reference_c4(args)
         return
     import oracle
     from sympiler_gb300 import matgen as mg
@@ -506,6 +568,168 @@ def bench_adjoint(dev, stream, flush, g=1024, k=32):
             "executors": {"forward": ef, "transposed": et}}
 
 
+def c4_shard(rank, world, dev):
+    """This rank's share of the 512-system batch (LPT on rows + entries), its
+    IC0 factors computed on the GPU in one pass over the shard's
+    block-diagonal pool, returned as per-system lower CSCs (the upper CSRs
+    IC0 works in): (indices, [(n, p, i, x)], rows, stored entries)."""
+    import torch
+    from sympiler_gb300 import matgen as mg
+    from sympiler_gb300 import plans
+    from sympiler_gb300.shard import shard_systems
+    systems = mg.batch_systems_upper(512, np.random.default_rng(44))
+    idx, mine = shard_systems(systems, rank, world)
+    N, up, ui, ux, off = mg.block_diagonal(mine)
+    dv = torch.from_numpy(ux).to(dev)
+    plans.ic0_device(N, dv, torch.from_numpy(up).to(dev), torch.from_numpy(ui).to(dev))
+    vals = dv.cpu().numpy()
+    fac, e0 = [], 0
+    for (n, p, i, x) in mine:
+        e1 = e0 + int(p[n])
+        fac.append((n, p, i, vals[e0:e1]))
+        e0 = e1
+    return idx, fac, N, int(up[-1])
+
+
+def c4_config(dt, k, nsys, world):
+    return {"workload": "C4 batch: 512 uneven SPD systems (80%% shifted 2D Laplacians 30..300 per side, 20%% "
+                        "random diagonally dominant, n 900..90,000), IC0 factors, forward SpTRSV, %d RHS %s, "
+                        "one batched sync-free launch per rank" % (k, dt.upper()),
+            "systems": 512, "systems_rank0": nsys, "rhs": k, "layout": "row-major (sum n_s) x k",
+            "l2": "inputs (about 1 GB in FP64) larger than L2; 256 MB L2 flush write between timed steps",
+            "parallelism": "systems sharded over %d rank(s) by LPT on rows + entries; no collective on the "
+                           "data path" % world}
+
+
+def run_c4(args):
+    """The batched workload as the timed step: each rank builds gbsym_batch
+    over its shard of the 512 systems and solves it with 8 right-hand sides;
+    value = algorithmic bytes of all ranks / the slowest rank's time."""
+    import torch
+    from sympiler_gb300 import plans
+    from sympiler_gb300._lib import EXEC_NAMES, LOWER_CSC
+    world, rank, local = dist_init()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    k, dt = 8, args.dtype
+    idx, fac, N, nnz = c4_shard(rank, world, dev)
+    if args.exec != "auto":  # one executor, no tuning (profiling runs)
+        os.environ["GBSYM_TRI_EXEC"] = args.exec
+    bp = plans.BatchPlan(fac, dtype=dt, kind=LOWER_CSC)
+    chosen = EXEC_NAMES.get(bp.autotune(k=k, dtype=dt)) if args.exec == "auto" else args.exec
+    info = bp.info()
+    vb = 8 if dt == "f64" else 4
+    byt = algorithmic_bytes(nnz, N, k, vb, vb)
+    tdt = torch.float64 if dt == "f64" else torch.float32
+    B = torch.from_numpy(np.random.default_rng(45 + rank).standard_normal((N, k))).to(dev).to(tdt)
+    X = torch.empty_like(B)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    stream = torch.cuda.current_stream()
+
+    def step(timed):
+        X.copy_(B)
+        flush.fill_(rank + 1)
+        if not timed:
+            bp.solve(X)
+            return None
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        bp.solve(X)
+        e1.record(stream)
+        return e0, e1
+
+    for _ in range(max(3, args.warmup)):
+        step(False)
+    bp.check()
+    sampler = ClockSampler(local)
+    sampler.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    launches0 = plans.kernel_launches()
+    evs = [step(True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    launches = plans.kernel_launches() - launches0
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = sampler.stop()
+    bp.check()
+    t_step = sum(a.elapsed_time(b) for a, b in evs) / len(evs) / 1e3
+    tot = torch.tensor([t_step, float(byt)], dtype=torch.float64, device=dev)
+    if world > 1:
+        tmax = tot[:1].clone()
+        torch.distributed.all_reduce(tmax, op=torch.distributed.ReduceOp.MAX)
+        bsum = tot[1:].clone()
+        torch.distributed.all_reduce(bsum)
+        t_step, byt_all = float(tmax.item()), float(bsum.item())
+    else:
+        byt_all = float(byt)
+    # residual spot check on this rank's first system (scipy, FP64)
+    import scipy.sparse as sp
+    n0, p0, i0, x0 = fac[0]
+    Lt0 = sp.csr_matrix((x0, i0, p0), shape=(n0, n0))
+    xs = X[:n0, 0].double().cpu().numpy()
+    resid = float(np.abs(Lt0.T @ xs - B[:n0, 0].double().cpu().numpy()).max())
+    # end to end: pinned host right-hand sides in, solution out, every step
+    Hb = torch.empty((N, k), dtype=tdt).pin_memory()
+    Hb.copy_(B.cpu())
+    Hx = torch.empty_like(Hb).pin_memory()
+
+    def e2e_once():
+        X.copy_(Hb, non_blocking=True)
+        bp.solve(X)
+        Hx.copy_(X, non_blocking=True)
+        torch.cuda.synchronize()
+    for _ in range(2):
+        e2e_once()
+    te = []
+    for _ in range(max(3, args.steps // 2)):
+        flush.fill_(rank + 1)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_once()
+        te.append(time.perf_counter() - t0)
+    e2e_t = statistics.median(te)
+    if world > 1:
+        tt = torch.tensor([e2e_t], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        e2e_t = float(tt.item())
+    peak, peak_src = hbm_peak()
+    if rank == 0:
+        line = {"metric": METRIC, "value": byt_all / t_step / 1e9, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+                "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": dt,
+                "data": "synthetic", "config": dict(c4_config(dt, k, len(idx), world), rows_rank0=N,
+                                                    levels_rank0=info.levels, executor=chosen),
+                "roofline": {"bound": "hbm", "achieved": byt / t_step / 1e9, "peak": peak, "unit": "GB/s",
+                             "frac": byt / t_step / 1e9 / peak, "peak_source": peak_src,
+                             "traffic": load_traffic("c4_batch_%s_8rhs" % dt),
+                             "algorithmic_bytes_per_solve": byt},
+                "e2e": {"value": byt_all / e2e_t / 1e9, "unit": UNIT, "h2d_bytes_per_step": N * k * vb,
+                        "d2h_bytes_per_step": N * k * vb, "ms_per_step": e2e_t * 1e3,
+                        "api": "BatchPlan.solve (gbsym_batch_solve) between pinned-host copies"},
+                "gpu_launches": int(launches), "clocks": clocks,
+                "check": {"max_abs_residual_system0_col0": resid}}
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def hbm_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            v = json.load(fh).get("hbm_gbs")
+            if v:
+                return float(v), "measured"
+    except (OSError, ValueError):
+        pass
+    return 6800.0, "fallback"
+
+
 def load_traffic(workload_key):
     p = os.path.join(ROOT, "profiles", "traffic.json")
     try:
@@ -519,6 +743,9 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.workload == "c4":
+        run_c4(args)
         return
     import torch
     world, rank, local = dist_init()

@@ -66,6 +66,7 @@ void choose_exec(gbsym_tri_s *t) {
   if (const char *pb = std::getenv("GBSYM_PERSIST_BLOCKS")) t->persist_blocks = std::atoi(pb);
   if (const char *cb = std::getenv("GBSYM_CLUSTER_BLOCKS")) t->cluster_blocks = std::atoi(cb);
   if (const char *sb = std::getenv("GBSYM_SF_BLOCKS_PER_SM")) t->sf_blocks_per_sm = std::atoi(sb);
+  if (const char *al = std::getenv("GBSYM_SF_ALT_LANES")) t->sf_alt_lanes = std::atoi(al) == 1;
   t->sf_deal = num_sms();
   if (const char *sd = std::getenv("GBSYM_SF_DEAL")) t->sf_deal = std::atoi(sd);
 }
@@ -118,13 +119,14 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   const long long m = (long long)t->n * k;
   DBuf<T> buf(m);
   // (executor, parameter) candidates: the sync-free sweep is tried at one,
-  // two and three blocks per SM (parameter bits 0-2) and, for several FP64
-  // right-hand sides, with lanes of one or two values per row (bit 3); the
-  // partitioned executor (k = 1 only) at several partition sizes
+  // two and three blocks per SM (parameter bits 0-2) and, for several
+  // right-hand sides, with its other lane layout (bit 3: two values per
+  // lane in FP64, one in FP32); the partitioned executor (k = 1 only) at
+  // several partition sizes
   std::vector<std::pair<int, int>> cands = {{GBSYM_EXEC_LEVELSET, 0}, {GBSYM_EXEC_PERSISTENT, 0},
                                             {GBSYM_EXEC_SYNCFREE, 1}, {GBSYM_EXEC_SYNCFREE, 2},
                                             {GBSYM_EXEC_SYNCFREE, 3}, {GBSYM_EXEC_CLUSTER, 0}};
-  if (k > 1 && sizeof(T) == 8)
+  if (k > 1)
     for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | 8});
   if (k == 1 && t->max_level_rows <= 4096) cands.push_back({GBSYM_EXEC_ONEBLOCK, 0});
   if (k == 1) {
@@ -148,13 +150,13 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   float best_ms = 0;
   const int saved_rows = t->part_rows_pref;
   const int kk = k > 1 ? 1 : 0;
-  const int saved_bps = t->sf_bps_tuned[kk], saved_pair = t->sf_pair_lanes;
+  const int saved_bps = t->sf_bps_tuned[kk], saved_alt = t->sf_alt_lanes;
   for (const auto &cand : cands) {
     const int e = cand.first;
     if (e == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = cand.second;
     if (e == GBSYM_EXEC_SYNCFREE) {
       t->sf_bps_tuned[kk] = cand.second & 7;
-      if (k > 1) t->sf_pair_lanes = cand.second >> 3;
+      if (k > 1) t->sf_alt_lanes = cand.second >> 3;
     }
     std::vector<float> ms;
     for (int rep = 0; rep < 4; ++rep) {
@@ -182,12 +184,12 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   cudaEventDestroy(e1);
   t->part_rows_pref = saved_rows;
   t->sf_bps_tuned[kk] = saved_bps;
-  t->sf_pair_lanes = saved_pair;
+  t->sf_alt_lanes = saved_alt;
   if (best < 0) throw Err{GBSYM_ERR_TIMEOUT};
   if (best == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = best_rows;
   if (best == GBSYM_EXEC_SYNCFREE) {
     t->sf_bps_tuned[kk] = best_rows & 7;
-    if (k > 1) t->sf_pair_lanes = best_rows >> 3;
+    if (k > 1) t->sf_alt_lanes = best_rows >> 3;
   }
   if (k == 1) t->exec = best; else t->exec_mrhs = best;
   std::lock_guard<std::mutex> lk(g_tuned_mu);

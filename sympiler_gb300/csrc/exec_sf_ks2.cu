@@ -1,10 +1,10 @@
 // exec_sf_ks2.cu -- the sync-free sweep's kernels compiled for a two-entry
-// slab (plans with t->K <= 2).
+// slab (plans with t->K <= 2) whose rows all fit in the slab.
 #include "exec_syncfree_kernel.cuh"
 
 namespace gbsym {
 
-template void sf_run_ks<double, 2>(gbsym_tri_s *, double *, double *, int, cudaStream_t);
-template void sf_run_ks<float, 2>(gbsym_tri_s *, float *, float *, int, cudaStream_t);
+template void sf_run_ks<double, 2, false>(gbsym_tri_s *, double *, double *, int, cudaStream_t);
+template void sf_run_ks<float, 2, false>(gbsym_tri_s *, float *, float *, int, cudaStream_t);
 
 }  // namespace gbsym

@@ -1,0 +1,11 @@
+// exec_sf_ks4_ov.cu -- the sync-free sweep's kernels compiled for a four-
+// entry slab (plans with t->K == 4) with rows longer than the slab (their
+// extra entries are polled and accumulated in groups).
+#include "exec_syncfree_kernel.cuh"
+
+namespace gbsym {
+
+template void sf_run_ks<double, 4, true>(gbsym_tri_s *, double *, double *, int, cudaStream_t);
+template void sf_run_ks<float, 4, true>(gbsym_tri_s *, float *, float *, int, cudaStream_t);
+
+}  // namespace gbsym

@@ -1,10 +1,11 @@
-// exec_sf_ks8.cu -- the sync-free sweep's kernels compiled for a full (kSlabMax-entry)
-// slab (plans with t->K > 4).
+// exec_sf_ks8.cu -- the sync-free sweep's kernels compiled for a full
+// (kSlabMax-entry) slab (plans with t->K > 4) whose rows all fit in the
+// slab.
 #include "exec_syncfree_kernel.cuh"
 
 namespace gbsym {
 
-template void sf_run_ks<double, kSlabMax>(gbsym_tri_s *, double *, double *, int, cudaStream_t);
-template void sf_run_ks<float, kSlabMax>(gbsym_tri_s *, float *, float *, int, cudaStream_t);
+template void sf_run_ks<double, kSlabMax, false>(gbsym_tri_s *, double *, double *, int, cudaStream_t);
+template void sf_run_ks<float, kSlabMax, false>(gbsym_tri_s *, float *, float *, int, cudaStream_t);
 
 }  // namespace gbsym

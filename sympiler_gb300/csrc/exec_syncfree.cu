@@ -55,13 +55,16 @@ void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
   t->sfy.reserve(bytes);
   T *y = reinterpret_cast<T *>(t->sfy.p);
   fill_sentinel(y, bytes, s);
+  const bool ov = t->nov > 0;
   switch (t->K) {
     case 0:
     case 1:
-    case 2: sf_run_ks<T, 2>(t, x, y, k, s); break;
-    case 3: sf_run_ks<T, 3>(t, x, y, k, s); break;
-    case 4: sf_run_ks<T, 4>(t, x, y, k, s); break;
-    default: sf_run_ks<T, kSlabMax>(t, x, y, k, s); break;
+    case 2: ov ? sf_run_ks<T, 2, true>(t, x, y, k, s) : sf_run_ks<T, 2, false>(t, x, y, k, s); break;
+    case 3: ov ? sf_run_ks<T, 3, true>(t, x, y, k, s) : sf_run_ks<T, 3, false>(t, x, y, k, s); break;
+    case 4: ov ? sf_run_ks<T, 4, true>(t, x, y, k, s) : sf_run_ks<T, 4, false>(t, x, y, k, s); break;
+    default:
+      ov ? sf_run_ks<T, kSlabMax, true>(t, x, y, k, s) : sf_run_ks<T, kSlabMax, false>(t, x, y, k, s);
+      break;
   }
 }
 

@@ -20,8 +20,9 @@ struct Units {
 Units sf_units(gbsym_tri_s *t, int rpw);
 
 // The sweep of a plan whose slab is at most KS entries wide (KS >= t->K),
-// into the sentinel-filled scratch y.
-template <class T, int KS>
+// into the sentinel-filled scratch y; OV: the plan has rows longer than its
+// slab.
+template <class T, int KS, bool OV>
 void sf_run_ks(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s);
 
 }  // namespace gbsym

@@ -101,6 +101,13 @@ __device__ __forceinline__ bool all_ready(const T (&v)[VEC]) {
 // Bounded waits count SM clock cycles (a register read, unlike the global
 // timer); 2^32 cycles is about two seconds at this part's clocks.
 __device__ __forceinline__ long long clock_now() { return clock64(); }
+
+// Entries past the slab are polled and accumulated this many at a time:
+// one L2 round trip per group instead of one per entry (rows longer than
+// the slab otherwise wait a round trip per extra entry, twice).  Two for
+// the kernels whose registers four would spill.
+template <class T, int VEC>
+constexpr int ov_batch() { return (sizeof(T) == 8 || VEC == 4) ? 2 : 4; }
 constexpr long long kWaitLimitCycles = 1ll << 32;
 
 // Position of this warp in the order units are dealt.  A cooperative grid
@@ -127,7 +134,10 @@ __device__ __forceinline__ int deal_warp(int nsm) {
 // slice once, in storage order.
 // A narrow slab (KS = 4) fits in 80 registers without spilling, which lets
 // three blocks share an SM; the full slab fits two blocks (128 registers).
-template <class T, int G, int VEC, int AR, int KS>
+// OVB: entries past the slab are polled and accumulated OVB at a time; a
+// plan without such entries runs the OVB = 0 kernel, which has no code
+// (and holds no registers) for them.
+template <class T, int G, int VEC, int AR, int KS, int OVB>
 __global__ void __launch_bounds__(kSfBlock, KS <= 4 ? 3 : 2)
 k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int *__restrict__ unit_row,
            const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
@@ -179,14 +189,26 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
             got |= 1u << q;
             moved = true;
           }
-        while (jo < rs.len) {
-          T v[VEC];
-          ld_rlx<T, VEC>(y + (size_t)A.oci[rs.ovb + jo - A.K] * k + r, v);
-          if (!all_ready<T, VEC>(v)) break;
-          ++jo;
-          moved = true;
+        // overflow dependencies, OVB per round: their column indices and
+        // values are loaded together, then taken in order while ready
+        if constexpr (OVB > 0) {
+          if (jo < rs.len) {
+            T v[OVB][VEC];
+#pragma unroll
+            for (int b = 0; b < OVB; ++b)
+              if (jo + b < rs.len) ld_rlx<T, VEC>(y + (size_t)A.oci[rs.ovb + jo + b - A.K] * k + r, v[b]);
+            bool run = true;
+#pragma unroll
+            for (int b = 0; b < OVB; ++b)
+              if (run && jo < rs.len && all_ready<T, VEC>(v[b])) {
+                ++jo;
+                moved = true;
+              } else {
+                run = false;
+              }
+          }
         }
-        if (got == need && jo >= rs.len) done = true;
+        if (got == need && (OVB == 0 || jo >= rs.len)) done = true;
         return moved;
       };
       if (kTwoRounds && !done) issue(va);
@@ -224,13 +246,24 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
 #pragma unroll
             for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], rs.v[q], xv[q][w]);
           }
-        for (int t = A.K; t < rs.len; ++t) {
-          const int e = rs.ovb + t - A.K;
-          T v[VEC];
-          ld_rlx<T, VEC>(y + (size_t)A.oci[e] * k + r, v);
-          const T a = A.ov[e];
+        // overflow entries in storage order, OVB loads in flight
+        if constexpr (OVB > 0) {
+          for (int t = A.K; t < rs.len; t += OVB) {
+            T v[OVB][VEC], a[OVB];
 #pragma unroll
-          for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], a, v[w]);
+            for (int b = 0; b < OVB; ++b)
+              if (t + b < rs.len) {
+                const int e = rs.ovb + t + b - A.K;
+                ld_rlx<T, VEC>(y + (size_t)A.oci[e] * k + r, v[b]);
+                a[b] = A.ov[e];
+              }
+#pragma unroll
+            for (int b = 0; b < OVB; ++b)
+              if (t + b < rs.len) {
+#pragma unroll
+                for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], a[b], v[b][w]);
+              }
+          }
         }
         T out[VEC];
 #pragma unroll
@@ -267,28 +300,33 @@ static void launch_coop(gbsym_tri_s *t, int k_of_launch, K kernel, cudaStream_t 
 // unrolled slab loops match the plan's slab width issues no guard
 // instructions for slots a row cannot have, which the polling loop repeats
 // every round (C2 64-RHS: 500 us at KS = 4 against 416 us at KS = 3).
-template <class T, int G, int AR, int KS>
+template <class T, int G, int AR, int KS, bool OV>
 static void sf_gk(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   const TriView<T> A = view_of<T>(t);
   const Units U = sf_units(t, 32 / G);
   // FP64 takes one value per lane: the polling then keeps two rounds of
   // loads in flight, which outweighs the narrower loads (measured 6-25%
   // faster for 8 to 64 right-hand sides on the C2 factor).  FP32 keeps
-  // 2- or 4-wide lanes, which measured faster there for 8 and 64.
+  // 2- or 4-wide lanes by default, which measured faster there for 8 and
+  // 64; the autotuner may choose one value per lane (sf_alt_lanes).
   if constexpr (sizeof(T) == 4) {
+    if (k > 1 && t->sf_alt_lanes == 1) {
+      launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+      return;
+    }
     if (k % 4 == 0 && (uintptr_t)x % 16 == 0) {
-      launch_coop(t, k, k_syncfree<T, G, 4, AR, KS>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+      launch_coop(t, k, k_syncfree<T, G, 4, AR, KS, OV ? ov_batch<T, 4>() : 0>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
     if (k % 2 == 0 && (uintptr_t)x % 8 == 0) {
-      launch_coop(t, k, k_syncfree<T, G, 2, AR, KS>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+      launch_coop(t, k, k_syncfree<T, G, 2, AR, KS, OV ? ov_batch<T, 2>() : 0>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
   }
-  launch_coop(t, k, k_syncfree<T, G, 1, AR, KS>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+  launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
 }
 
-template <class T, int AR, int KS>
+template <class T, int AR, int KS, bool OV>
 static void sf_ar(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   if (k == 1) {
     // one right-hand side: 8 rows per warp unit (4 lanes each, one active).
@@ -296,7 +334,7 @@ static void sf_ar(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
     // fewer rows per unit shorten that wait; fewer than 8 costs more in
     // FP64 issue slots than it saves (measured on the C2 and C3 factors:
     // 8 rows 4-5% faster than 32, 1 row twice as slow)
-    sf_gk<T, 4, AR, KS>(t, x, y, k, s);
+    sf_gk<T, 4, AR, KS, OV>(t, x, y, k, s);
     return;
   }
   // FP64 lanes carry one value each, so by default a row takes the next
@@ -304,23 +342,24 @@ static void sf_ar(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   // 32 right-hand sides (C2: 8 RHS 260 -> 246 us, 32 RHS 325 -> 308 us
   // against half as many lanes, each taking two slices).  Which is faster
   // depends on the matrix (the C4 batch prefers half at 8 RHS), so the
-  // autotuner chooses (sf_pair_lanes).  FP32 lanes carry two or four.
+  // autotuner chooses (sf_alt_lanes).  FP32 lanes carry two or four values
+  // by default, one (as many lanes as FP64's default) as the alternative.
   int g64 = 2;
   while (g64 < k && g64 < 32) g64 <<= 1;
-  const bool pair = t->sf_pair_lanes == 1;
-  switch (sizeof(T) == 8 && !pair ? g64 : lanes_for(k, sizeof(T))) {
-    case 2: sf_gk<T, 2, AR, KS>(t, x, y, k, s); break;
-    case 4: sf_gk<T, 4, AR, KS>(t, x, y, k, s); break;
-    case 8: sf_gk<T, 8, AR, KS>(t, x, y, k, s); break;
-    case 16: sf_gk<T, 16, AR, KS>(t, x, y, k, s); break;
-    default: sf_gk<T, 32, AR, KS>(t, x, y, k, s); break;
+  const bool alt = t->sf_alt_lanes == 1;
+  switch ((sizeof(T) == 8) != alt ? g64 : lanes_for(k, sizeof(T))) {
+    case 2: sf_gk<T, 2, AR, KS, OV>(t, x, y, k, s); break;
+    case 4: sf_gk<T, 4, AR, KS, OV>(t, x, y, k, s); break;
+    case 8: sf_gk<T, 8, AR, KS, OV>(t, x, y, k, s); break;
+    case 16: sf_gk<T, 16, AR, KS, OV>(t, x, y, k, s); break;
+    default: sf_gk<T, 32, AR, KS, OV>(t, x, y, k, s); break;
   }
 }
 
-template <class T, int KS>
+template <class T, int KS, bool OV>
 void sf_run_ks(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
-  if (t->arith == kArithFused) sf_ar<T, kArithFused, KS>(t, x, y, k, s);
-  else sf_ar<T, kArithExact, KS>(t, x, y, k, s);
+  if (t->arith == kArithFused) sf_ar<T, kArithFused, KS, OV>(t, x, y, k, s);
+  else sf_ar<T, kArithExact, KS, OV>(t, x, y, k, s);
 }
 
 }  // namespace gbsym

@@ -314,6 +314,27 @@ def tri_adjoint(Lt: TriPlan, n, Lp, Li, X, g, grad, stream=None):
     return g, grad
 
 
+def batch_arguments(systems):
+    """The C-ABI arguments of gbsym_batch_create(_kind) for a list of
+    (n, p, i, x) host systems: (nsys, n[], p[], i[], x[], keepalive)."""
+    nsys = len(systems)
+    keep = []
+    ns = (C.c_int * nsys)()
+    ps = (C.c_void_p * nsys)()
+    is_ = (C.c_void_p * nsys)()
+    xs = (C.c_void_p * nsys)()
+    for q, (n, p, i, x) in enumerate(systems):
+        p = np.ascontiguousarray(p, dtype=np.int32)
+        i = np.ascontiguousarray(i, dtype=np.int32)
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        keep += [p, i, x]
+        ns[q] = int(n)
+        ps[q] = p.ctypes.data
+        is_[q] = i.ctypes.data
+        xs[q] = x.ctypes.data
+    return nsys, ns, ps, is_, xs, keep
+
+
 class BatchPlan:
     """Many triangular systems of uneven sizes solved together: lower CSRs
     with the diagonal last (kind LOWER_DIAG_LAST, the default) or lower CSCs
@@ -321,26 +342,12 @@ class BatchPlan:
     arrays."""
 
     def __init__(self, systems, dtype="f64", kind=L.LOWER_DIAG_LAST, stream=None):
-        nsys = len(systems)
-        self._keep = []
-        ns = (C.c_int * nsys)()
-        ps = (C.c_void_p * nsys)()
-        is_ = (C.c_void_p * nsys)()
-        xs = (C.c_void_p * nsys)()
-        for q, (n, p, i, x) in enumerate(systems):
-            p = np.ascontiguousarray(p, dtype=np.int32)
-            i = np.ascontiguousarray(i, dtype=np.int32)
-            x = np.ascontiguousarray(x, dtype=np.float64)
-            self._keep += [p, i, x]
-            ns[q] = int(n)
-            ps[q] = p.ctypes.data
-            is_[q] = i.ctypes.data
-            xs[q] = x.ctypes.data
+        nsys, ns, ps, is_, xs, keep = batch_arguments(systems)
         h = C.c_void_p()
         check(lib().gbsym_batch_create_kind(C.byref(h), nsys, ns, ps, is_, xs, int(kind), _dtype_code(dtype),
                                             _stream(stream)), "gbsym_batch_create_kind")
+        del keep
         self._h = h
-        self._keep = None
         self.nsys = nsys
         self.dtype = _dtype_code(dtype)
         off = np.zeros(nsys + 1, dtype=np.int64)

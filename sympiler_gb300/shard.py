@@ -35,3 +35,12 @@ def partition_systems(costs: Sequence[int], world: int) -> List[List[int]]:
 
 def rank_systems(costs: Sequence[int], rank: int, world: int) -> List[int]:
     return partition_systems(costs, world)[rank]
+
+
+def shard_systems(systems: Sequence, rank: int, world: int):
+    """The rank's share of a batch of (n, p, i, x) systems: (indices,
+    systems), placed by partition_systems on each system's rows plus stored
+    entries."""
+    costs = [system_cost(s[0], int(s[1][s[0]]) if s[0] else 0) for s in systems]
+    idx = partition_systems(costs, world)[rank]
+    return idx, [systems[q] for q in idx]

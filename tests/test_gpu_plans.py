@@ -242,6 +242,38 @@ def test_syncfree_every_slab_width(gpu, orc, w):
     assert np.array_equal(x32.cpu().numpy(), ref32), w
 
 
+@pytest.mark.parametrize("alt", ["0", "1"])
+@pytest.mark.parametrize("w", [3, 5])
+def test_syncfree_lane_layouts_fp32_fp64(gpu, orc, monkeypatch, w, alt):
+    """Both lane layouts of the multi-RHS sync-free sweep (FP64: one or two
+    values per lane; FP32: two/four or one), with and without rows past the
+    slab: FP64 bit-exact against the oracle, FP32 against the FP32 oracle
+    column by column."""
+    from sympiler_gb300._lib import EXEC_SYNCFREE
+    from sympiler_gb300.plans import TriPlan
+    monkeypatch.setenv("GBSYM_SF_ALT_LANES", alt)
+    rng = np.random.default_rng(300 + w)
+    for L in (_banded_lower(3001, w, seed=w), _banded_with_long_rows(3001, w, seed=w)):
+        for dt in ("f64", "f32"):
+            plan = TriPlan(L.n, *L.astuple(), dtype=dt)
+            plan.set_exec(EXEC_SYNCFREE)
+            for k in (3, 8, 64):
+                B = rng.standard_normal((L.n, k))
+                if dt == "f64":
+                    ref = _oracle_mrhs(orc, L, B)
+                else:
+                    B = B.astype(np.float32)
+                    ref = np.empty_like(B)
+                    for c in range(k):
+                        r = np.ascontiguousarray(B[:, c])
+                        orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), r)
+                        ref[:, c] = r
+                x = torch.from_numpy(B.copy()).cuda()
+                plan.solve(x)
+                plan.check()
+                assert np.array_equal(x.cpu().numpy(), ref), (w, dt, k, alt)
+
+
 def test_autotune_picks_a_working_executor(gpu, orc, c2_factor):
     from sympiler_gb300.plans import TriPlan
     _, L, _ = c2_factor

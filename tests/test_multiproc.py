@@ -1,7 +1,10 @@
 """Multi-rank placement of a batch of independent systems, run as two gloo
 ranks on CPU: every system lands on exactly one rank, the loads balance,
-and each rank's shard is solved independently (oracle arithmetic, no data
-exchanged) to the same answer a single rank gives."""
+each rank packs its shard into the batch plan's C-ABI arguments (the code
+the multi-GPU benchmark runs before gbsym_batch_create_kind) and the
+library's host-side argument checks accept them and reject a corrupted
+copy, and each rank's shard is solved independently (oracle arithmetic, no
+data exchanged) to the same answer a single rank gives."""
 import os
 import socket
 
@@ -11,7 +14,7 @@ import torch.distributed as dist
 import torch.multiprocessing as mp
 
 from sympiler_gb300 import matgen as mg
-from sympiler_gb300.shard import partition_systems, system_cost
+from sympiler_gb300.shard import partition_systems, shard_systems, system_cost
 
 
 def _free_port():
@@ -37,10 +40,30 @@ def _worker(rank, world, port, result_dir):
     dist.init_process_group("gloo", rank=rank, world_size=world)
     import oracle
     import torch
+    import ctypes as C
+
+    from sympiler_gb300._lib import ERR_BAD_MATRIX, LOWER_DIAG_LAST, F64, lib
+    from sympiler_gb300.plans import batch_arguments
     orc = oracle.orc()
     systems = _systems()
     costs = [system_cost(L.n, L.nnz) for L in systems]
     mine = partition_systems(costs, world)[rank]
+    # the benchmark's shard-to-batch-plan path, host side
+    idx, shard = shard_systems([(L.n, *L.astuple()) for L in systems], rank, world)
+    assert idx == mine
+    nsys, ns, ps, is_, xs, keep = batch_arguments(shard)
+    assert nsys == len(mine) and [ns[q] for q in range(nsys)] == [systems[q].n for q in mine]
+    for (n, p, i, x) in shard:
+        assert p[0] == 0 and p[n] == len(i) and i.min() >= 0 and i.max() < n
+    # a shard whose system has a column outside it is refused before any device work
+    n0, p0, i0, x0 = shard[0]
+    bad_i = i0.copy()
+    bad_i[p0[1] - 1] = n0  # the first row's diagonal now points past its system
+    bad = [(n0, p0, bad_i, x0)] + list(shard[1:])
+    nb, nsb, psb, isb, xsb, keepb = batch_arguments(bad)
+    h = C.c_void_p()
+    st = lib().gbsym_batch_create_kind(C.byref(h), nb, nsb, psb, isb, xsb, LOWER_DIAG_LAST, F64, None)
+    assert st == ERR_BAD_MATRIX and not h.value
     # each rank solves only its systems; nothing is exchanged on the data path
     sums = np.zeros(len(systems))
     for q in mine:
