@@ -362,40 +362,45 @@ def _time(fn, reps, stream, flush=None):
     return statistics.median(ts)
 
 
-def bench_batch(dev, stream, flush, nsys=512, k=8):
-    """512 uneven SPD systems (80% shifted 2D Laplacians on 30..300 grids,
-    20% random diagonally dominant, n 900..90,000), IC0 on the GPU, all
-    systems solved in one executor pass with 8 right-hand sides."""
+def bench_batch(dev, stream, flush, hop_us=None, k=8):
+    """The 512 uneven SPD systems (80% shifted 2D Laplacians on 30..300
+    grids, 20% random diagonally dominant, n 900..90,000), IC0 on the GPU,
+    solved with 8 right-hand sides through the batch API (gbsym_batch_*) in
+    one executor pass, FP64 and FP32.  Floors: HBM (algorithmic bytes at the
+    measured copy bandwidth) and level latency (the pool's levels x hop_us,
+    the per-level hop of the one-RHS FP32 sweep on the C2 factor)."""
     import torch
-    from sympiler_gb300 import matgen as mg
     from sympiler_gb300 import plans
-    from sympiler_gb300._lib import LOWER_CSC
+    from sympiler_gb300._lib import EXEC_NAMES, LOWER_CSC
     t0 = time.perf_counter()
-    systems = mg.batch_systems_upper(nsys, np.random.default_rng(44))
-    N, up, ui, ux, off = mg.block_diagonal(systems)
-    dp, di = torch.from_numpy(up).to(dev), torch.from_numpy(ui).to(dev)
-    dv = torch.from_numpy(ux).to(dev)
-    plans.ic0_device(N, dv, dp, di)          # IC0 of every system at once
-    res = {"systems": nsys, "rows": N, "nnz_L": int(up[-1]), "setup_s": None}
+    idx, fac, N, nnz = c4_shard(0, 1, dev)
+    res = {"systems": len(idx), "rows": N, "nnz_L": nnz, "setup_s": None, "api": "gbsym_batch_create_kind / "
+           "gbsym_batch_autotune / gbsym_batch_solve"}
     rng = np.random.default_rng(45)
+    peak, src = hbm_peak()
     for dt in ("f64", "f32"):
-        P = plans.TriPlan(N, dp, di, dv, kind=LOWER_CSC, dtype=dt)
+        bp = plans.BatchPlan(fac, dtype=dt, kind=LOWER_CSC)
         tdt = torch.float64 if dt == "f64" else torch.float32
         B = torch.from_numpy(rng.standard_normal((N, k))).to(dev).to(tdt)
         X = torch.empty_like(B)
-        chosen = P.autotune(k=k, dtype=dt)
-        info = P.info()
+        chosen = EXEC_NAMES.get(bp.autotune(k=k, dtype=dt))
+        info = bp.info()
 
         def run():
             X.copy_(B)
-            P.solve(X)
+            bp.solve(X)
         run()
-        t = _time(run, 5, stream, flush)
-        vb, sb = (8, 8) if dt == "f64" else (4, 4)
-        byt = algorithmic_bytes(int(info.nnz_off) + N, N, k, vb, sb)
+        t = _time(run, 5, stream, flush) - _time(lambda: X.copy_(B), 5, stream, flush)
+        bp.check()
+        vb = 8 if dt == "f64" else 4
+        byt = algorithmic_bytes(nnz, N, k, vb, vb)
         res[dt] = {"ms": t * 1e3, "batch_solves_per_s": 1.0 / t, "gbs": byt / t / 1e9,
-                   "levels": info.levels, "executor": chosen}
-        del P, B, X
+                   "frac": byt / t / 1e9 / peak, "peak_gbs": peak, "peak_source": src,
+                   "levels": info.levels, "executor": chosen, "hbm_floor_ms": byt / peak / 1e6}
+        if hop_us:
+            res[dt]["floor_ms"] = max(byt / peak / 1e6, info.levels * hop_us / 1e3)
+            res[dt]["floor_note"] = "max(HBM floor, levels x %.2f us one-RHS FP32 hop on the C2 factor)" % hop_us
+        del bp, B, X
     res["setup_s"] = time.perf_counter() - t0
     return res
 
@@ -524,6 +529,38 @@ def bench_supernodal(dev, stream, flush, grid=64):
     return out
 
 
+def fp32_mrhs(L, dev, stream, flush, k=64):
+    """FP32 storage and vectors, k right-hand sides, out of place, on a lower
+    CSR factor: time, GB/s and fraction of HBM, with two floors: the HBM
+    floor (algorithmic bytes at the measured copy bandwidth) and the
+    level-latency floor (levels x the per-level hop of the one-RHS FP32
+    sweep on the same factor, measured here)."""
+    import torch
+    from sympiler_gb300._lib import EXEC_NAMES
+    from sympiler_gb300.plans import TriPlan
+    P = TriPlan(L.n, *L.astuple(), dtype="f32")
+    ek = EXEC_NAMES.get(P.autotune(k=k, dtype="f32"))
+    e1 = EXEC_NAMES.get(P.autotune(k=1, dtype="f32"))
+    rng = np.random.default_rng(64)
+    B = torch.from_numpy(rng.standard_normal((L.n, k)).astype(np.float32)).to(dev)
+    X = torch.empty_like(B)
+    b1 = B[:, 0].contiguous()
+    x1 = torch.empty_like(b1)
+    tk = _time(lambda: P.solve_into(B, X), 7, stream, flush)
+    t1 = _time(lambda: P.solve_into(b1, x1), 7, stream, flush)
+    P.check()
+    levels = P.info().levels
+    peak, src = hbm_peak()
+    byt = algorithmic_bytes(L.nnz, L.n, k, 4, 4)
+    return {"n": L.n, "nnz_L": int(L.nnz), "levels": levels, "rhs": k, "ms": tk * 1e3, "gbs": byt / tk / 1e9,
+            "frac": byt / tk / 1e9 / peak, "peak_gbs": peak, "peak_source": src,
+            "algorithmic_bytes": byt, "hbm_floor_ms": byt / peak / 1e6,
+            "floor_ms": t1 * 1e3, "hop_us": t1 * 1e6 / levels,
+            "floor_note": "level-latency floor = levels x the per-level hop of the one-RHS FP32 sync-free "
+                          "sweep on the same factor (%.1f us measured)" % (t1 * 1e6),
+            "executors": {"k%d" % k: ek, "k1": e1}}
+
+
 def bench_adjoint(dev, stream, flush, g=1024, k=32):
     """Forward X = L^{-1} B and the reverse pass (L^T solve + value gradient)
     on the IC0 factor of the 1024^2 anisotropic variable-coefficient Poisson
@@ -563,7 +600,8 @@ def bench_adjoint(dev, stream, flush, g=1024, k=32):
     tb = _time(bwd, 5, stream, flush)
     info = Lf.info()
     byt = algorithmic_bytes(Lcsr.nnz, U.n, k)
-    return {"n": U.n, "nnz_L": Lcsr.nnz, "levels": info.levels, "rhs": k,
+    fp32 = fp32_mrhs(Lcsr, dev, stream, flush, 64)
+    return {"fp32_64rhs": fp32, "n": U.n, "nnz_L": Lcsr.nnz, "levels": info.levels, "rhs": k,
             "forward_ms": tf * 1e3, "forward_gbs": byt / tf / 1e9, "backward_ms": tb * 1e3,
             "executors": {"forward": ef, "transposed": et}}
 
@@ -796,17 +834,19 @@ def main():
     result = {}
 
     if not args.extras_only:
+        # one step: X = L^-1 B out of place (gbsym_tri_solve_into), B
+        # resident and unchanged; the sync-free sweep publishes each result
+        # straight into X
         def step(timed):
-            X.copy_(B)
             flush.fill_(rank + 1)
             if timed:
                 e0 = torch.cuda.Event(enable_timing=True)
                 e1 = torch.cuda.Event(enable_timing=True)
                 e0.record(stream)
-                plan.solve(X)
+                plan.solve_into(B, X)
                 e1.record(stream)
                 return e0, e1
-            plan.solve(X)
+            plan.solve_into(B, X)
             return None
 
         for _ in range(max(3, args.warmup)):
@@ -892,6 +932,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": dict(config(g, k), levels=info.levels, nnz_L=int(L.nnz), executor=tuned,
                            arithmetic="exact (reference operation order, bit-identical)",
+                           api="gbsym_tri_solve_into: X = L^-1 B out of place, B unchanged",
                            wall_s_timed_region=wall),
             "roofline": {"bound": "hbm", "achieved": byt / t_step / 1e9, "peak": peak, "unit": "GB/s",
                          "frac": byt / t_step / 1e9 / peak, "peak_source": peak_src,
@@ -899,7 +940,7 @@ def main():
                          "algorithmic_bytes_per_solve": byt,
                          "note": ("one solve = one graph of per-level kernels"
                                   if tuned["k%d" % k] == "levelset" else
-                                  "one solve = one %s kernel launch" % tuned["k%d" % k])
+                                  "one solve = the sentinel fill of X + one %s kernel launch" % tuned["k%d" % k])
                                  + "; duration from CUDA events on the launch stream"},
             "roofline_fp64": {"bound": "fp64 pipe", "achieved": fp64_ops_exact(int(info.nnz_off), n, k) / t_step / 1e9,
                               "peak": FP64_PEAK_GOPS, "unit": "G FP64 op/s",
@@ -976,6 +1017,16 @@ def main():
         ex["autotuned"] = {"k1": EXEC_NAMES.get(plan.autotune(k=1)),
                            "k%d" % k: EXEC_NAMES.get(plan.autotune(k=k))}
         extras["executors"] = ex
+        # the same factor in FP32 with 64 right-hand sides
+        extras["sptrsv_64rhs_fp32_c2"] = fp32_mrhs(L, dev, stream, flush, 64)
+        # in place (gbsym_tri_solve) beside the out-of-place headline step
+        def in_place():
+            X.copy_(B)
+            plan.solve(X)
+        t_ip = _time(in_place, 7, stream, flush)
+        t_cp = _time(lambda: X.copy_(B), 7, stream, flush)
+        extras["sptrsv_%drhs_in_place" % k] = {"ms_incl_copy": t_ip * 1e3, "copy_ms": t_cp * 1e3,
+                                               "ms": (t_ip - t_cp) * 1e3}
         # IC0-PCG to 1e-10 on C2 (FP64 throughout)
         Pt = TriPlan(n, *Lt.astuple(), kind=UPPER_DIAG_FIRST)
         Pt.autotune(k=1)
@@ -1021,7 +1072,24 @@ def main():
                 xg.zero_()
                 runs.append(plans.gmres(Cp, Lu, Up, bc, xg, mr=30, maxit=100, tol=1e-10))
             best = min(runs, key=lambda r: r.seconds)
-            out[prec] = {"seconds": best.seconds, "iterations": best.iterations, "restarts": best.restarts,
+            # per-iteration split: one preconditioner apply (the two
+            # triangular sweeps, in the plan's precision), one system SpMV,
+            # and the rest (Gram-Schmidt passes, the device Givens step,
+            # precision conversions, launch gaps)
+            tdt = torch.float32 if prec == "f32" else torch.float64
+            zsrc = bc.to(tdt)
+            zz = torch.empty_like(zsrc)
+
+            def apply_once():
+                Lu.solve_into(zsrc, zz)
+                Up.solve(zz)
+            t_apply = _time(apply_once, 7, stream, flush)
+            t_spmv = _time(lambda: Cp.spmv(bc, xg), 7, stream, flush)
+            it_ms = best.seconds / max(1, best.iterations) * 1e3
+            split = {"iteration_ms": it_ms, "precond_apply_ms": t_apply * 1e3, "spmv_ms": t_spmv * 1e3,
+                     "rest_ms": it_ms - t_apply * 1e3 - t_spmv * 1e3}
+            out[prec] = {"per_iteration": split,
+                         "seconds": best.seconds, "iterations": best.iterations, "restarts": best.restarts,
                          "relres": best.relres, "status": best.status, "executors": tuned_prec}
         out["speedup_fp32_precond"] = out["f64"]["seconds"] / out["f32"]["seconds"]
         # the same GMRES on one host core: the restated driver over the
@@ -1044,8 +1112,9 @@ def main():
             out["cpu_port"] = {"error": str(ex)}
         extras["gmres_c3"] = out
         del Cp, dC, lu
-        extras["batch_c4"] = bench_batch(dev, stream, flush)
+        extras["batch_c4"] = bench_batch(dev, stream, flush, extras["sptrsv_64rhs_fp32_c2"]["hop_us"])
         extras["adjoint_c5"] = bench_adjoint(dev, stream, flush)
+        extras["sptrsv_64rhs_fp32_c5"] = extras["adjoint_c5"].pop("fp32_64rhs")
         extras["spmv"] = bench_spmv(dev, stream, flush)
         extras["supernodal_c2_nd"] = bench_supernodal(dev, stream, flush)
         result["extras"] = extras

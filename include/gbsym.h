@@ -71,6 +71,21 @@ void gbsym_free(void *p);
 /* Number of kernels this library has launched in this process so far. */
 unsigned long long gbsym_kernel_launches(void);
 
+/* Drop-in plan cache.  No counterpart in the reference: its executors keep
+ * nothing between calls, while a drop-in here uploads the matrix, checks it
+ * and builds a plan on every call.  capacity > 0 lets the drop-ins keep up
+ * to that many plans (least recently used evicted), keyed by the device,
+ * the matrix kind, n, the entry count, the array pointers (values,
+ * indices, diagonal pointers, schedule arrays) and the caller's version;
+ * a later call with the same key reuses the plan and uploads only x.  The
+ * cache checks nothing else: whenever the caller changes a cached matrix's
+ * arrays in place it must pass a new version to
+ * gbsym_dropin_cache_version, which drops every cached plan.  capacity 0
+ * (the default) turns the cache off and frees the plans not in use.
+ * Returns GBSYM_ERR_SIZE for a negative capacity. */
+int gbsym_dropin_cache(int capacity);
+void gbsym_dropin_cache_version(unsigned long long version);
+
 /* ---- drop-ins: SpTRSV, CSR row-pull ------------------------------------- */
 /* sparse_blas/sptrsv.cpp:17-25 ; include/sympiler/sparse_blas_lib.h:126-127 */
 void gbsym_sptrsv_csr(int n, int *Lp, int *Li, double *Lx, double *x);
@@ -443,10 +458,20 @@ int gbsym_selftest_bounded_wait(long long limit_ns, void *stream);
 int gbsym_tri_get_schedule(gbsym_tri t, int *level_ptr, int *level_set);
 
 /* Solve in place on device memory: x holds k right-hand sides in the given
- * layout and dtype (FP64 or FP32 vectors).  An FP32 solve requires FP32
- * value storage; an FP64 solve accepts either.  Stream-ordered. */
+ * layout and dtype (FP64 or FP32 vectors, matching the plan's value
+ * storage).  Stream-ordered. */
 int gbsym_tri_solve(gbsym_tri t, void *x, int k, int layout, int dtype,
                     void *stream);
+/* Out of place on device memory: x = L^-1 b for k row-major right-hand
+ * sides (n x k, dtype matching the plan's value storage); b is left
+ * unchanged and must not overlap x (b == x solves in place).  The results
+ * are bit-identical to gbsym_tri_solve's.  The sync-free executor reads b
+ * and publishes each result straight into x, so it writes the solution
+ * once instead of twice; a solution value whose bits are all ones (a NaN
+ * carried from a NaN input) is stored as the default NaN.  The other
+ * executors copy b into x and solve in place.  Stream-ordered. */
+int gbsym_tri_solve_into(gbsym_tri t, const void *b, void *x, int k, int dtype,
+                         void *stream);
 /* The lbc_redundant row formula: x_i = ((0 - sum_j L_ij x_j) + b_i)/L_ii. */
 int gbsym_tri_solve_b(gbsym_tri t, const double *b, double *x, void *stream);
 /* End-to-end: x is HOST memory (pinned or pageable); the call returns when

@@ -33,6 +33,8 @@ SIGNATURES = {
     "gbsym_status_string": (C.c_char_p, [_int]),
     "gbsym_free": (None, [_vp]),
     "gbsym_kernel_launches": (_ull, []),
+    "gbsym_dropin_cache": (_int, [_int]),
+    "gbsym_dropin_cache_version": (None, [_ull]),
     # drop-ins
     "gbsym_sptrsv_csr": (None, [_int, _vp, _vp, _vp, _vp]),
     "gbsym_sptrsv_csr_ilu": (None, [_int, _vp, _vp, _vp, _vp, _vp]),
@@ -72,6 +74,7 @@ SIGNATURES = {
     "gbsym_tri_get_schedule": (_int, [_vp, _vp, _vp]),
     "gbsym_tri_solve": (_int, [_vp, _vp, _int, _int, _int, _vp]),
     "gbsym_tri_solve_b": (_int, [_vp, _vp, _vp, _vp]),
+    "gbsym_tri_solve_into": (_int, [_vp, _vp, _vp, _int, _int, _vp]),
     "gbsym_tri_solve_host": (_int, [_vp, _vp, _int, _int]),
     "gbsym_host_solve_in_place": (_int, [_vp]),
     "gbsym_tree_levelset": (_int, [_int, _vp, _vp, _vp]),

@@ -10,7 +10,9 @@
 // API instead, which keeps the matrix resident.
 #include <algorithm>
 #include <cstdlib>
+#include <cstring>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 #include "common.cuh"
@@ -64,6 +66,105 @@ struct HostLbc {
   const int *level_ptr, *par_ptr, *partition;
 };
 
+// ---------------------------------------------------------------------------
+// Opt-in plan cache of the drop-ins.  A reference caller that solves with
+// one matrix in a loop (Cholesky::solve, the demo's repeated runs) would
+// otherwise pay for the upload, the validation and the plan build on every
+// call.  With the cache on, a drop-in whose arguments name the same arrays
+// (the same pointers, n, entry count, kind and schedule arrays) on the same
+// device under the same caller version reuses the plan it built the first
+// time, after checking nothing: the caller declares, by changing the
+// version, that any cached matrix's arrays changed in place.  Plans are
+// evicted least recently used beyond the capacity.  A cached plan is used
+// by one call at a time (its own lock); other matrices proceed in parallel.
+struct CacheKey {
+  int dev = 0, kind = 0, n = 0, nnz = 0, levels = 0;
+  const void *ptr[8] = {};
+  unsigned long long version = 0;
+  bool operator==(const CacheKey &o) const {
+    return dev == o.dev && kind == o.kind && n == o.n && nnz == o.nnz && levels == o.levels &&
+           version == o.version && std::memcmp(ptr, o.ptr, sizeof(ptr)) == 0;
+  }
+};
+struct CachedPlan {
+  CacheKey key;
+  std::unique_ptr<gbsym_tri_s> plan;
+  std::mutex use;
+  unsigned long long last = 0;
+};
+static std::mutex g_cache_mu;
+static std::vector<std::shared_ptr<CachedPlan>> g_cache;
+static int g_cache_cap = 0;
+static unsigned long long g_cache_version = 0, g_cache_clock = 0;
+
+static CacheKey cache_key(int n, int nnz, int kind, const void *p, const void *i, const void *v,
+                          const void *diags, const HostLevels *lv, const HostLbc *lbc) {
+  CacheKey k;
+  GB_CUDA(cudaGetDevice(&k.dev));
+  k.kind = kind;
+  k.n = n;
+  k.nnz = nnz;
+  k.ptr[0] = p;
+  k.ptr[1] = i;
+  k.ptr[2] = v;
+  k.ptr[3] = diags;
+  if (lv) {
+    k.levels = lv->levels;
+    k.ptr[4] = lv->ptr;
+    k.ptr[5] = lv->set;
+  }
+  if (lbc) {
+    k.levels = -1 - lbc->level_no;
+    k.ptr[4] = lbc->level_ptr;
+    k.ptr[5] = lbc->par_ptr;
+    k.ptr[6] = lbc->partition;
+  }
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  k.version = g_cache_version;
+  return k;
+}
+
+static std::shared_ptr<CachedPlan> cache_find(const CacheKey &k) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  if (g_cache_cap <= 0) return nullptr;
+  for (auto &e : g_cache)
+    if (e->key == k) {
+      e->last = ++g_cache_clock;
+      return e;
+    }
+  return nullptr;
+}
+
+static void cache_put(const CacheKey &k, std::unique_ptr<gbsym_tri_s> plan) {
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  if (g_cache_cap <= 0 || k.version != g_cache_version) return;
+  auto e = std::make_shared<CachedPlan>();
+  e->key = k;
+  e->plan = std::move(plan);
+  e->last = ++g_cache_clock;
+  g_cache.push_back(std::move(e));
+  while ((int)g_cache.size() > g_cache_cap) {
+    auto lru = std::min_element(g_cache.begin(), g_cache.end(),
+                                [](const std::shared_ptr<CachedPlan> &a, const std::shared_ptr<CachedPlan> &b) {
+                                  return a->last < b->last;
+                                });
+    g_cache.erase(lru);  // a call still using it keeps it alive
+  }
+}
+
+// Solve on a plan the cache holds: upload x (and b), solve, download.
+static void cached_solve(CachedPlan &c, int n, double *x, const double *b, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(c.use);
+  DBuf<double> dx, db;
+  upload(dx, x, n, false, s);
+  if (b) upload(db, b, n, false, s);
+  tri_solve_rowmajor(c.plan.get(), dx.p, b ? db.p : nullptr, 1, GBSYM_F64, s);
+  const int code = tri_read_error(c.plan.get(), s);
+  if (code) throw Err{code};
+  GB_CUDA(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  GB_CUDA(cudaStreamSynchronize(s));
+}
+
 // Solve one triangle stored as (p, i, v[, diags]) of the given kind, in
 // place on host x (b non-null: the redundant row formula).
 static void tri_dropin(int n, const int *p, const int *i, const double *v, const int *diags,
@@ -75,6 +176,11 @@ static void tri_dropin(int n, const int *p, const int *i, const double *v, const
   cudaStream_t s = thread_stream();
   const int nnz = p[n];
   GB_CHECK(nnz >= 0, GBSYM_ERR_BAD_MATRIX);
+  const CacheKey key = cache_key(n, nnz, kind, p, i, v, diags, lv, lbc);
+  if (auto c = cache_find(key)) {
+    cached_solve(*c, n, x, b, s);
+    return;
+  }
   DBuf<int> dp, di, dd, dls;
   DBuf<double> dv, dx, db;
   upload(dp, p, n + 1, false, s);
@@ -97,6 +203,7 @@ static void tri_dropin(int n, const int *p, const int *i, const double *v, const
   if (code) throw Err{code};
   GB_CUDA(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
+  cache_put(key, std::move(t));
 }
 
 // Lower-triangular CSC (diagonal first in each column) -> CSR pull form
@@ -148,6 +255,11 @@ static void csc_dropin(int n, const int *Lp, const int *Li, const double *Lx, do
   if (n == 0) return;
   GB_CHECK(Lp && Li && Lx && x, GBSYM_ERR_NULL_ARG);
   cudaStream_t s = thread_stream();
+  const CacheKey key = cache_key(n, Lp[n], GBSYM_LOWER_CSC, Lp, Li, Lx, nullptr, lv, lbc);
+  if (auto c = cache_find(key)) {
+    cached_solve(*c, n, x, nullptr, s);
+    return;
+  }
   DevCsr L;
   csc_lower_to_csr(n, Lp, Li, Lx, L, s);
   DBuf<int> dls;
@@ -165,6 +277,7 @@ static void csc_dropin(int n, const int *Lp, const int *Li, const double *Lx, do
   if (code) throw Err{code};
   GB_CUDA(cudaMemcpyAsync(x, dx.p, n * sizeof(double), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
+  cache_put(key, std::move(t));
 }
 
 __global__ void k_div_by_vec(double *__restrict__ x, const double *__restrict__ d, int n) {
@@ -317,6 +430,28 @@ void *gbsym_alloc(size_t bytes) { return bytes ? std::malloc(bytes) : nullptr; }
 void gbsym_free(void *p) { std::free(p); }
 
 unsigned long long gbsym_kernel_launches(void) { return g_launches.load(); }
+
+int gbsym_dropin_cache(int capacity) {
+  if (capacity < 0) return GBSYM_ERR_SIZE;
+  std::vector<std::shared_ptr<CachedPlan>> dropped;
+  {
+    std::lock_guard<std::mutex> lk(g_cache_mu);
+    g_cache_cap = capacity;
+    while ((int)g_cache.size() > capacity) {
+      dropped.push_back(std::move(g_cache.back()));
+      g_cache.pop_back();
+    }
+  }
+  return GBSYM_OK;  // plans not in use are freed here, as `dropped` goes
+}
+
+void gbsym_dropin_cache_version(unsigned long long version) {
+  std::vector<std::shared_ptr<CachedPlan>> dropped;
+  std::lock_guard<std::mutex> lk(g_cache_mu);
+  if (version == g_cache_version) return;
+  g_cache_version = version;
+  dropped.swap(g_cache);  // no entry can match any more
+}
 
 // ---- SpTRSV CSR -----------------------------------------------------------
 void gbsym_sptrsv_csr(int n, int *Lp, int *Li, double *Lx, double *x) {

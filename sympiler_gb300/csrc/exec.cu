@@ -76,7 +76,7 @@ static void solve_as(gbsym_tri_s *t, int e, T *x, const T *b, int k, int dtype, 
   switch (e) {
     case GBSYM_EXEC_ONEBLOCK: run_oneblock<T>(t, x, s); break;
     case GBSYM_EXEC_PERSISTENT: run_persist<T>(t, x, k, s); break;
-    case GBSYM_EXEC_SYNCFREE: run_syncfree<T>(t, x, k, s); break;
+    case GBSYM_EXEC_SYNCFREE: run_syncfree<T>(t, x, k, s, nullptr); break;
     case GBSYM_EXEC_CLUSTER: run_cluster<T>(t, x, k, s); break;
     case GBSYM_EXEC_PARTITIONED: run_part<T>(t, x, s); break;
     default: run_levelset<T>(t, x, b, k, dtype, s); break;
@@ -97,6 +97,20 @@ void tri_solve_rowmajor(gbsym_tri_s *t, void *x, const void *b, int k, int dtype
     GB_CHECK(t->vdtype == GBSYM_F32 && b == nullptr, GBSYM_ERR_UNSUPPORTED);
     solve_typed<float>(t, (float *)x, nullptr, k, dtype, s);
   }
+}
+
+void tri_solve_into(gbsym_tri_s *t, const void *b, void *x, int k, int dtype, cudaStream_t s) {
+  if (t->n == 0 || k == 0) return;
+  GB_CHECK((dtype == GBSYM_F64) == (t->vdtype == GBSYM_F64), GBSYM_ERR_UNSUPPORTED);
+  if (effective_exec(t, k, false) == GBSYM_EXEC_SYNCFREE) {
+    // the sweep reads b and publishes each result straight into x
+    if (dtype == GBSYM_F64) run_syncfree<double>(t, (double *)x, k, s, (const double *)b);
+    else run_syncfree<float>(t, (float *)x, k, s, (const float *)b);
+    return;
+  }
+  const size_t es = dtype == GBSYM_F64 ? sizeof(double) : sizeof(float);
+  GB_CUDA(cudaMemcpyAsync(x, b, (size_t)t->n * k * es, cudaMemcpyDeviceToDevice, s));
+  tri_solve_rowmajor(t, x, nullptr, k, dtype, s);
 }
 
 int tri_read_error(gbsym_tri_s *t, cudaStream_t s) {

@@ -236,8 +236,11 @@ template <class T>
 void run_persist(gbsym_tri_s *t, T *x, int k, cudaStream_t s);
 template <class T>
 void run_oneblock(gbsym_tri_s *t, T *x, cudaStream_t s);
+// b non-null: out of place, x = L^-1 b with b left unchanged; the solution
+// is published straight into x (sentinel-filled first) instead of into the
+// plan's scratch copy.
 template <class T>
-void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s);
+void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s, const T *b);
 template <class T>
 void run_part(gbsym_tri_s *t, T *x, cudaStream_t s);
 template <class T>

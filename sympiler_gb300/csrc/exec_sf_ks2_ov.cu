@@ -5,7 +5,7 @@
 
 namespace gbsym {
 
-template void sf_run_ks<double, 2, true>(gbsym_tri_s *, double *, double *, int, cudaStream_t);
-template void sf_run_ks<float, 2, true>(gbsym_tri_s *, float *, float *, int, cudaStream_t);
+template void sf_run_ks<double, 2, true>(gbsym_tri_s *, double *, double *, const double *, int, cudaStream_t);
+template void sf_run_ks<float, 2, true>(gbsym_tri_s *, float *, float *, const float *, int, cudaStream_t);
 
 }  // namespace gbsym

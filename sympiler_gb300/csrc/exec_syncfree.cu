@@ -50,25 +50,28 @@ void fill_sentinel(void *y, size_t bytes, cudaStream_t s) {
 }
 
 template <class T>
-void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
+void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s, const T *b) {
   const size_t bytes = (size_t)t->n * k * sizeof(T);
-  t->sfy.reserve(bytes);
-  T *y = reinterpret_cast<T *>(t->sfy.p);
+  T *y = x;
+  if (!b) {
+    t->sfy.reserve(bytes);
+    y = reinterpret_cast<T *>(t->sfy.p);
+  }
   fill_sentinel(y, bytes, s);
   const bool ov = t->nov > 0;
   switch (t->K) {
     case 0:
     case 1:
-    case 2: ov ? sf_run_ks<T, 2, true>(t, x, y, k, s) : sf_run_ks<T, 2, false>(t, x, y, k, s); break;
-    case 3: ov ? sf_run_ks<T, 3, true>(t, x, y, k, s) : sf_run_ks<T, 3, false>(t, x, y, k, s); break;
-    case 4: ov ? sf_run_ks<T, 4, true>(t, x, y, k, s) : sf_run_ks<T, 4, false>(t, x, y, k, s); break;
+    case 2: ov ? sf_run_ks<T, 2, true>(t, x, y, b, k, s) : sf_run_ks<T, 2, false>(t, x, y, b, k, s); break;
+    case 3: ov ? sf_run_ks<T, 3, true>(t, x, y, b, k, s) : sf_run_ks<T, 3, false>(t, x, y, b, k, s); break;
+    case 4: ov ? sf_run_ks<T, 4, true>(t, x, y, b, k, s) : sf_run_ks<T, 4, false>(t, x, y, b, k, s); break;
     default:
-      ov ? sf_run_ks<T, kSlabMax, true>(t, x, y, k, s) : sf_run_ks<T, kSlabMax, false>(t, x, y, k, s);
+      ov ? sf_run_ks<T, kSlabMax, true>(t, x, y, b, k, s) : sf_run_ks<T, kSlabMax, false>(t, x, y, b, k, s);
       break;
   }
 }
 
-template void run_syncfree<double>(gbsym_tri_s *, double *, int, cudaStream_t);
-template void run_syncfree<float>(gbsym_tri_s *, float *, int, cudaStream_t);
+template void run_syncfree<double>(gbsym_tri_s *, double *, int, cudaStream_t, const double *);
+template void run_syncfree<float>(gbsym_tri_s *, float *, int, cudaStream_t, const float *);
 
 }  // namespace gbsym

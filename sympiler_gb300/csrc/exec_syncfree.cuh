@@ -20,9 +20,10 @@ struct Units {
 Units sf_units(gbsym_tri_s *t, int rpw);
 
 // The sweep of a plan whose slab is at most KS entries wide (KS >= t->K),
-// into the sentinel-filled scratch y; OV: the plan has rows longer than its
-// slab.
+// into the sentinel-filled y; OV: the plan has rows longer than its slab.
+// In place (b null) y is the plan's scratch copy and x receives every value
+// as well; out of place y is x itself and the right-hand sides come from b.
 template <class T, int KS, bool OV>
-void sf_run_ks(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s);
+void sf_run_ks(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s);
 
 }  // namespace gbsym

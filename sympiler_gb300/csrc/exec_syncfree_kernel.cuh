@@ -139,8 +139,12 @@ __device__ __forceinline__ int deal_warp(int nsm) {
 // (and holds no registers) for them.
 template <class T, int G, int VEC, int AR, int KS, int OVB>
 __global__ void __launch_bounds__(kSfBlock, KS <= 4 ? 3 : 2)
-k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int *__restrict__ unit_row,
+k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ unit_row,
            const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
+  // in place (b null): right-hand sides from x, results to x and published
+  // to y; out of place: right-hand sides from b, results published to y = x
+  const T *rhs = b ? b : x;
+  const bool store_x = y != x;
   constexpr unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int gl = lane % G;
@@ -162,7 +166,7 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
       const unsigned need = (1u << ns) - 1u;
       int jo = A.K;          // next overflow dependency
       T acc[VEC];
-      if (!done) vload<T, VEC, false>(x + (size_t)rs.orig * k + r, acc);
+      if (!done) vload<T, VEC, false>(rhs + (size_t)rs.orig * k + r, acc);
       long long t0 = clock_now();
       int rounds = 0;
       // With one value per lane, polling keeps two rounds of slab loads in
@@ -271,7 +275,7 @@ k_syncfree(TriView<T> A, T *__restrict__ x, T *__restrict__ y, int k, const int 
           acc[w] = row_finish(A, rs, acc[w]);
           out[w] = not_sentinel(acc[w]);
         }
-        vstore<T, VEC>(x + (size_t)rs.orig * k + r, acc);
+        if (store_x) vstore<T, VEC>(x + (size_t)rs.orig * k + r, acc);
         st_rlx<T, VEC>(y + (size_t)rs.orig * k + r, out);
       }
     }
@@ -301,7 +305,7 @@ static void launch_coop(gbsym_tri_s *t, int k_of_launch, K kernel, cudaStream_t 
 // instructions for slots a row cannot have, which the polling loop repeats
 // every round (C2 64-RHS: 500 us at KS = 4 against 416 us at KS = 3).
 template <class T, int G, int AR, int KS, bool OV>
-static void sf_gk(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
+static void sf_gk(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s) {
   const TriView<T> A = view_of<T>(t);
   const Units U = sf_units(t, 32 / G);
   // FP64 takes one value per lane: the polling then keeps two rounds of
@@ -311,30 +315,30 @@ static void sf_gk(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   // 64; the autotuner may choose one value per lane (sf_alt_lanes).
   if constexpr (sizeof(T) == 4) {
     if (k > 1 && t->sf_alt_lanes == 1) {
-      launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+      launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
-    if (k % 4 == 0 && (uintptr_t)x % 16 == 0) {
-      launch_coop(t, k, k_syncfree<T, G, 4, AR, KS, OV ? ov_batch<T, 4>() : 0>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+    if (k % 4 == 0 && ((uintptr_t)x | (uintptr_t)(b ? b : x)) % 16 == 0) {
+      launch_coop(t, k, k_syncfree<T, G, 4, AR, KS, OV ? ov_batch<T, 4>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
-    if (k % 2 == 0 && (uintptr_t)x % 8 == 0) {
-      launch_coop(t, k, k_syncfree<T, G, 2, AR, KS, OV ? ov_batch<T, 2>() : 0>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+    if (k % 2 == 0 && ((uintptr_t)x | (uintptr_t)(b ? b : x)) % 8 == 0) {
+      launch_coop(t, k, k_syncfree<T, G, 2, AR, KS, OV ? ov_batch<T, 2>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
   }
-  launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+  launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
 }
 
 template <class T, int AR, int KS, bool OV>
-static void sf_ar(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
+static void sf_ar(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s) {
   if (k == 1) {
     // one right-hand side: 8 rows per warp unit (4 lanes each, one active).
     // A unit waits for all its rows' dependencies before computing, so
     // fewer rows per unit shorten that wait; fewer than 8 costs more in
     // FP64 issue slots than it saves (measured on the C2 and C3 factors:
     // 8 rows 4-5% faster than 32, 1 row twice as slow)
-    sf_gk<T, 4, AR, KS, OV>(t, x, y, k, s);
+    sf_gk<T, 4, AR, KS, OV>(t, x, y, b, k, s);
     return;
   }
   // FP64 lanes carry one value each, so by default a row takes the next
@@ -348,18 +352,18 @@ static void sf_ar(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
   while (g64 < k && g64 < 32) g64 <<= 1;
   const bool alt = t->sf_alt_lanes == 1;
   switch ((sizeof(T) == 8) != alt ? g64 : lanes_for(k, sizeof(T))) {
-    case 2: sf_gk<T, 2, AR, KS, OV>(t, x, y, k, s); break;
-    case 4: sf_gk<T, 4, AR, KS, OV>(t, x, y, k, s); break;
-    case 8: sf_gk<T, 8, AR, KS, OV>(t, x, y, k, s); break;
-    case 16: sf_gk<T, 16, AR, KS, OV>(t, x, y, k, s); break;
-    default: sf_gk<T, 32, AR, KS, OV>(t, x, y, k, s); break;
+    case 2: sf_gk<T, 2, AR, KS, OV>(t, x, y, b, k, s); break;
+    case 4: sf_gk<T, 4, AR, KS, OV>(t, x, y, b, k, s); break;
+    case 8: sf_gk<T, 8, AR, KS, OV>(t, x, y, b, k, s); break;
+    case 16: sf_gk<T, 16, AR, KS, OV>(t, x, y, b, k, s); break;
+    default: sf_gk<T, 32, AR, KS, OV>(t, x, y, b, k, s); break;
   }
 }
 
 template <class T, int KS, bool OV>
-void sf_run_ks(gbsym_tri_s *t, T *x, T *y, int k, cudaStream_t s) {
-  if (t->arith == kArithFused) sf_ar<T, kArithFused, KS, OV>(t, x, y, k, s);
-  else sf_ar<T, kArithExact, KS, OV>(t, x, y, k, s);
+void sf_run_ks(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s) {
+  if (t->arith == kArithFused) sf_ar<T, kArithFused, KS, OV>(t, x, y, b, k, s);
+  else sf_ar<T, kArithExact, KS, OV>(t, x, y, b, k, s);
 }
 
 }  // namespace gbsym

@@ -250,8 +250,10 @@ __device__ __forceinline__ void last_block_sums(int m, const double *pdot, doubl
 __global__ void __launch_bounds__(kRedThreads)
 k_mgs_pass_sum(long long n, double *__restrict__ v, const double *__restrict__ vprev,
                const double *__restrict__ hprev, const double *__restrict__ vnext, double *__restrict__ pdot,
-               double *__restrict__ pnorm, double *out_dot, double *out_norm, unsigned *ticket) {
+               double *__restrict__ pnorm, double *out_dot, double *out_norm, unsigned *ticket,
+               const int *__restrict__ run_if) {
   __shared__ double sh[32];
+  if (run_if && *run_if == 0) return;  // a re-orthogonalisation pass that is not needed
   const double h = vprev ? *hprev : 0.0;
   double sd = 0.0, sn = 0.0;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
@@ -273,6 +275,106 @@ k_mgs_pass_sum(long long n, double *__restrict__ v, const double *__restrict__ v
     if (threadIdx.x == 0) pnorm[blockIdx.x] = sn;
   }
   last_block_sums(gridDim.x, pdot, out_dot, pnorm, out_norm, ticket, sh);
+}
+
+// v = alpha[0] * v, alpha read on the device
+__global__ void k_scale_by(long long n, const double *__restrict__ alpha, double *__restrict__ v) {
+  const double a = *alpha;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    v[i] = a * v[i];
+}
+
+// ---- the small Hessenberg problem, on the device ---------------------------
+// One thread; at most mr + 1 = 31 rows.  Every product and sum is rounded
+// separately (no contraction), as the reference's host code computes it.
+//
+// State (doubles): H[(mr+1) x mr] row-major, c[mr+1], sn[mr+1], g[mr+1],
+// y[mr+1], then the per-step words below.
+enum { GW_SCALE = 0, GW_RHO, GW_CONV, GW_BREAK, GW_COUNT };
+
+struct GmresState {
+  double *H, *c, *sn, *g, *y, *w;  // w: GW_COUNT words
+  int *reorth;                     // re-orthogonalise this step (0/1)
+  int mr;
+};
+
+__device__ __forceinline__ double mul_(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_(double a, double b) { return __dsub_rn(a, b); }
+
+// After the first Gram-Schmidt round of step k: column k of H from the
+// dots, and the re-orthogonalisation test av + delta * h(k+1,k) == av
+// (mgmres.cpp:901-925).
+__global__ void k_gm_column(GmresState st, int k, const double *__restrict__ sc, double delta) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int mr = st.mr;
+  const double av = sqrt(sc[mr + 1]);
+  for (int j = 0; j <= k; ++j) st.H[j * mr + k] = sc[j];
+  const double h = sqrt(sc[k + 1]);
+  st.H[(k + 1) * mr + k] = h;
+  *st.reorth = add_(av, mul_(delta, h)) == av ? 1 : 0;
+}
+
+// After the (possibly skipped) second round: its dots added to column k,
+// the scale of v_{k+1}, the earlier rotations applied to column k, the new
+// rotation (mgmres.cpp:927-958, mult_givens 186-251), |g[k+1]| and the
+// convergence and breakdown words.
+__global__ void k_gm_givens(GmresState st, int k, const double *__restrict__ sc, double rho_tol) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int mr = st.mr;
+  double *H = st.H;
+  auto Hm = [&](int i, int j) -> double & { return H[i * mr + j]; };
+  if (*st.reorth) {
+    for (int j = 0; j <= k; ++j) Hm(j, k) = add_(Hm(j, k), sc[j]);
+    Hm(k + 1, k) = sqrt(sc[k + 1]);
+  }
+  const double hn = Hm(k + 1, k);
+  st.w[GW_SCALE] = hn != 0.0 ? 1.0 / hn : 1.0;
+  for (int j = 0; j < k; ++j) {
+    const double a = Hm(j, k), b = Hm(j + 1, k);
+    Hm(j, k) = sub_(mul_(st.c[j], a), mul_(st.sn[j], b));
+    Hm(j + 1, k) = add_(mul_(st.sn[j], a), mul_(st.c[j], b));
+  }
+  const double mu = sqrt(add_(mul_(Hm(k, k), Hm(k, k)), mul_(Hm(k + 1, k), Hm(k + 1, k))));
+  if (mu == 0.0) {
+    st.w[GW_BREAK] = 1.0;
+    st.w[GW_CONV] = 0.0;
+    return;
+  }
+  st.c[k] = Hm(k, k) / mu;
+  st.sn[k] = -Hm(k + 1, k) / mu;
+  Hm(k, k) = sub_(mul_(st.c[k], Hm(k, k)), mul_(st.sn[k], Hm(k + 1, k)));
+  Hm(k + 1, k) = 0.0;
+  const double g1 = sub_(mul_(st.c[k], st.g[k]), mul_(st.sn[k], st.g[k + 1]));
+  const double g2 = add_(mul_(st.sn[k], st.g[k]), mul_(st.c[k], st.g[k + 1]));
+  st.g[k] = g1;
+  st.g[k + 1] = g2;
+  const double rho = fabs(g2);
+  st.w[GW_RHO] = rho;
+  st.w[GW_CONV] = rho <= rho_tol ? 1.0 : 0.0;
+  st.w[GW_BREAK] = 0.0;
+}
+
+// Restart set-up: g = rho e_1 (mgmres.cpp:878-886); H, c, sn need no
+// clearing (every entry is written before it is read).
+__global__ void k_gm_start(GmresState st, const double *__restrict__ rr) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int i = 0; i <= st.mr; ++i) st.g[i] = 0.0;
+  st.g[0] = sqrt(rr[0]);
+}
+
+// Back substitution on the rotated H (mgmres.cpp:960-972) into y[0..k].
+__global__ void k_gm_backsub(GmresState st, int k) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int mr = st.mr;
+  auto Hm = [&](int i, int j) { return st.H[i * mr + j]; };
+  st.y[k] = st.g[k] / Hm(k, k);
+  for (int i = k - 1; i >= 0; --i) {
+    double t = st.g[i];
+    for (int j = i + 1; j < k + 1; ++j) t = sub_(t, mul_(Hm(i, j), st.y[j]));
+    st.y[i] = t / Hm(i, i);
+  }
 }
 
 // w = sum_j y[j] V[j]
@@ -311,20 +413,25 @@ struct Precond {
   }
 };
 
-static void mult_givens(double c, double sn, int k, double *g) {
-  const double g1 = c * g[k] - sn * g[k + 1];
-  const double g2 = sn * g[k] + c * g[k + 1];
-  g[k] = g1;
-  g[k + 1] = g2;
-}
-
+// GMRES(mr) with the Arnoldi step's small problem on the device.  Per step
+// k the host only launches: the preconditioner and the SpMV, the Gram-
+// Schmidt passes (the second round's passes run only when k_gm_column asked
+// for them), k_gm_givens and the scaling of v_{k+1}; then it copies step
+// k's three words (rho, converged, breakdown) to pinned memory.  The host
+// reads step k-1's words after launching step k, so the GPU never waits for
+// the host inside a restart cycle; when step k-1 has converged the already
+// queued step k does no harm (it touches H's column k, g[k+1..k+2] and
+// v_{k+1}, none of which the back substitution of step k-1 reads) and its
+// time is the cost of the one-step lag.
 void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, double *x, int mr,
            int maxit, double tol, gbsym_krylov_result *res, cudaStream_t s) {
   const long long n = A->n;
   GB_CHECK(mr >= 1 && Lu->n == n && U->n == n && Lu->vdtype == U->vdtype, GBSYM_ERR_SIZE);
   const double t0 = now_s();
   const double delta = 1.0e-03;
-  DBuf<double> V((size_t)(mr + 1) * n), r(n), w(n), sc(2 * (mr + 2)), dy(mr + 1);
+  DBuf<double> V((size_t)(mr + 1) * n), r(n), w(n), sc(2 * (mr + 2));
+  DBuf<double> st_buf((size_t)(mr + 1) * mr + 4 * (mr + 1) + GW_COUNT);
+  DBuf<int> reorth(1);
   DBuf<double> pd, pn;
   DBuf<unsigned> ticket(1);
   Reducer red;
@@ -333,11 +440,29 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
   pd.alloc(blocks);
   pn.alloc(blocks);
   GB_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s));
+  GmresState st;
+  st.H = st_buf.p;
+  st.c = st.H + (size_t)(mr + 1) * mr;
+  st.sn = st.c + (mr + 1);
+  st.g = st.sn + (mr + 1);
+  st.y = st.g + (mr + 1);
+  st.w = st.y + (mr + 1);
+  st.reorth = reorth.p;
+  st.mr = mr;
+  // pinned words: [0] the residual norm^2 of a restart, then GW_COUNT per step
   double *hs = nullptr;
-  GB_CUDA(cudaMallocHost((void **)&hs, 2 * (mr + 2) * sizeof(double)));
+  const size_t hwords = 1 + (size_t)GW_COUNT * mr;
+  GB_CUDA(cudaMallocHost((void **)&hs, hwords * sizeof(double)));
   std::unique_ptr<double, void (*)(double *)> hs_guard(hs, [](double *v) { cudaFreeHost(v); });
-  std::vector<double> H((size_t)(mr + 1) * mr), c(mr + 1), sn(mr + 1), g(mr + 1), y(mr + 1);
-  auto Hm = [&](int i, int j) -> double & { return H[(size_t)i * mr + j]; };
+  std::vector<cudaEvent_t> ev(mr, nullptr);
+  struct EvGuard {
+    std::vector<cudaEvent_t> &e;
+    ~EvGuard() {
+      for (auto x : e)
+        if (x) cudaEventDestroy(x);
+    }
+  } ev_guard{ev};
+  for (auto &e : ev) GB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   auto Vj = [&](int j) { return V.p + (size_t)j * n; };
   const int eb = ew_blocks(n);
   // ||b||
@@ -348,6 +473,25 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
   int itr_used = 0, restarts = 0;
   double rho = 0.0, rho_tol = 0.0;
   bool converged = false, breakdown = false;
+  // one Gram-Schmidt round over v = v_{k+1}: pass j (0..k) applies
+  // projection j-1 and dots with v_j, pass k+1 applies projection k and
+  // takes the norm.  First round: sc[j] <- h[j][k], sc[k+1] <- ||v||^2,
+  // sc[mr+1] <- ||v||^2 before orthogonalisation (av).  Second round (only
+  // if k_gm_column set the flag): the same without av.
+  auto mgs_round = [&](int k, bool second) {
+    double *v = Vj(k + 1);
+    for (int j = 0; j <= k + 1; ++j) {
+      const double *vprev = j > 0 ? Vj(j - 1) : nullptr;
+      const double *vnext = j <= k ? Vj(j) : nullptr;
+      double *norm = nullptr;
+      if (!second && (j == 0 || j == k + 1)) norm = sc.p + (j == 0 ? mr + 1 : k + 1);
+      if (second && j == k + 1) norm = sc.p + k + 1;
+      k_mgs_pass_sum<<<blocks, kRedThreads, 0, s>>>(n, v, vprev, sc.p + (j > 0 ? j - 1 : 0), vnext, pd.p, pn.p,
+                                                    vnext ? sc.p + j : nullptr, norm, ticket.p,
+                                                    second ? reorth.p : nullptr);
+      check_launch();
+    }
+  };
   for (int itr = 0; itr < maxit && !converged && !breakdown; ++itr) {
     csr_spmv(A, x, r.p, GBSYM_F64, s);
     k_residual<<<eb, 256, 0, s>>>(n, b, r.p);
@@ -364,89 +508,55 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
     ++restarts;
     k_scale<<<eb, 256, 0, s>>>(n, 1.0 / rho, r.p, Vj(0));
     check_launch();
-    g.assign(mr + 1, 0.0);
-    g[0] = rho;
-    std::fill(H.begin(), H.end(), 0.0);
-    int k = 0, k_copy = 0;
-    for (k = 0; k < mr; ++k) {
-      k_copy = k;
+    k_gm_start<<<1, 32, 0, s>>>(st, sc.p);
+    check_launch();
+    int k_last = -1;    // last step launched
+    int k_stop = -1;    // step that converged, or -1
+    int k_break = -1;   // step that broke down, or -1
+    auto inspect = [&](int k) {
+      GB_CUDA(cudaEventSynchronize(ev[k]));
+      const double *hw = hs + 1 + (size_t)GW_COUNT * k;
+      if (hw[GW_BREAK] != 0.0) k_break = k;
+      else if (hw[GW_CONV] != 0.0) k_stop = k;
+      if (hw[GW_BREAK] == 0.0) rho = hw[GW_RHO];
+    };
+    for (int k = 0; k < mr; ++k) {
       // v_{k+1} = A M^-1 v_k
       M.apply(Vj(k), w.p, n, s);
       csr_spmv(A, w.p, Vj(k + 1), GBSYM_F64, s);
-      double *v = Vj(k + 1);
-      // pass j (0..k): apply projection j-1, dot with v_j; pass k+1: apply
-      // projection k, norm.  sc[j] <- h[j][k]; sc[k+1] <- ||v||^2 ;
-      // sc[mr+1] <- ||v||^2 before orthogonalisation (av).
-      for (int j = 0; j <= k + 1; ++j) {
-        const double *vprev = j > 0 ? Vj(j - 1) : nullptr;
-        const double *vnext = j <= k ? Vj(j) : nullptr;
-        const bool norm = j == 0 || j == k + 1;
-        k_mgs_pass_sum<<<blocks, kRedThreads, 0, s>>>(n, v, vprev, sc.p + (j > 0 ? j - 1 : 0), vnext, pd.p, pn.p,
-                                                      vnext ? sc.p + j : nullptr,
-                                                      norm ? sc.p + (j == 0 ? mr + 1 : k + 1) : nullptr, ticket.p);
-        check_launch();
-      }
-      GB_CUDA(cudaMemcpyAsync(hs, sc.p, (mr + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
-      GB_CUDA(cudaStreamSynchronize(s));
-      const double av = std::sqrt(hs[mr + 1]);
-      for (int j = 0; j <= k; ++j) Hm(j, k) = hs[j];
-      Hm(k + 1, k) = std::sqrt(hs[k + 1]);
-      if (av + delta * Hm(k + 1, k) == av) {
-        // re-orthogonalise once more, accumulating into h
-        for (int j = 0; j <= k + 1; ++j) {
-          const double *vprev = j > 0 ? Vj(j - 1) : nullptr;
-          const double *vnext = j <= k ? Vj(j) : nullptr;
-          k_mgs_pass_sum<<<blocks, kRedThreads, 0, s>>>(n, v, vprev, sc.p + (j > 0 ? j - 1 : 0), vnext, pd.p,
-                                                        pn.p, vnext ? sc.p + j : nullptr,
-                                                        j == k + 1 ? sc.p + k + 1 : nullptr, ticket.p);
-          check_launch();
-        }
-        GB_CUDA(cudaMemcpyAsync(hs, sc.p, (mr + 2) * sizeof(double), cudaMemcpyDeviceToHost, s));
-        GB_CUDA(cudaStreamSynchronize(s));
-        for (int j = 0; j <= k; ++j) Hm(j, k) += hs[j];
-        Hm(k + 1, k) = std::sqrt(hs[k + 1]);
-      }
-      if (Hm(k + 1, k) != 0.0) {
-        k_scale<<<eb, 256, 0, s>>>(n, 1.0 / Hm(k + 1, k), v, v);
-        check_launch();
-      }
+      mgs_round(k, false);
+      k_gm_column<<<1, 32, 0, s>>>(st, k, sc.p, delta);
+      check_launch();
+      mgs_round(k, true);
+      k_gm_givens<<<1, 32, 0, s>>>(st, k, sc.p, rho_tol);
+      check_launch();
+      k_scale_by<<<eb, 256, 0, s>>>(n, st.w + GW_SCALE, Vj(k + 1));
+      check_launch();
+      GB_CUDA(cudaMemcpyAsync(hs + 1 + (size_t)GW_COUNT * k, st.w, GW_COUNT * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
+      GB_CUDA(cudaEventRecord(ev[k], s));
+      k_last = k;
       if (k > 0) {
-        for (int i = 0; i < k + 2; ++i) y[i] = Hm(i, k);
-        for (int j = 0; j < k; ++j) mult_givens(c[j], sn[j], j, y.data());
-        for (int i = 0; i < k + 2; ++i) Hm(i, k) = y[i];
-      }
-      const double mu = std::sqrt(Hm(k, k) * Hm(k, k) + Hm(k + 1, k) * Hm(k + 1, k));
-      if (mu == 0.0) {  // the reference returns here without updating x
-        breakdown = true;
-        break;
-      }
-      c[k] = Hm(k, k) / mu;
-      sn[k] = -Hm(k + 1, k) / mu;
-      Hm(k, k) = c[k] * Hm(k, k) - sn[k] * Hm(k + 1, k);
-      Hm(k + 1, k) = 0.0;
-      mult_givens(c[k], sn[k], k, g.data());
-      rho = std::fabs(g[k + 1]);
-      ++itr_used;
-      if (rho <= rho_tol) {
-        converged = true;
-        break;
+        inspect(k - 1);  // step k is queued behind it
+        if (k_stop >= 0 || k_break >= 0) break;
       }
     }
-    if (breakdown) break;
-    k = std::min(k_copy, mr - 1);
-    y[k] = g[k] / Hm(k, k);
-    for (int i = k - 1; i >= 0; --i) {
-      y[i] = g[i];
-      for (int j = i + 1; j < k + 1; ++j) y[i] -= Hm(i, j) * y[j];
-      y[i] /= Hm(i, i);
+    if (k_stop < 0 && k_break < 0) inspect(k_last);
+    if (k_break >= 0) {  // the reference returns here without updating x
+      itr_used += k_break;
+      breakdown = true;
+      break;
     }
-    GB_CUDA(cudaMemcpyAsync(dy.p, y.data(), (k + 1) * sizeof(double), cudaMemcpyHostToDevice, s));
-    k_combine<<<eb, 256, 0, s>>>(n, k + 1, V.p, n, dy.p, r.p);
+    const int kk = k_stop >= 0 ? k_stop : k_last;
+    itr_used += kk + 1;
+    if (k_stop >= 0) converged = true;
+    k_gm_backsub<<<1, 32, 0, s>>>(st, kk);
+    check_launch();
+    k_combine<<<eb, 256, 0, s>>>(n, kk + 1, V.p, n, st.y, r.p);
     check_launch();
     M.apply(r.p, w.p, n, s);
     k_add<<<eb, 256, 0, s>>>(n, w.p, x);
     check_launch();
-    GB_CUDA(cudaStreamSynchronize(s));  // y is reused on the host
   }
   // final FP64 residual
   csr_spmv(A, x, r.p, GBSYM_F64, s);

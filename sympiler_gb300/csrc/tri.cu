@@ -567,7 +567,7 @@ void gather_values(long long m, const double *src, const int *idx, double *dst, 
 }
 
 template <class T>
-void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s);  // exec_syncfree.cu
+void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s, const T *b);  // exec_syncfree.cu
 
 }  // namespace gbsym
 
@@ -714,6 +714,16 @@ extern "C" int gbsym_tri_solve(gbsym_tri t, void *x, int k, int layout, int dtyp
   });
 }
 
+extern "C" int gbsym_tri_solve_into(gbsym_tri t, const void *b, void *x, int k, int dtype, void *stream) {
+  if (!t || (t->n && k > 0 && (!x || !b))) return GBSYM_ERR_NULL_ARG;
+  if (k < 0) return GBSYM_ERR_SIZE;
+  return guarded([&] {
+    cudaStream_t s = (cudaStream_t)stream;
+    if (b == x) tri_solve_rowmajor(t, x, nullptr, k, dtype, s);
+    else tri_solve_into(t, b, x, k, dtype, s);
+  });
+}
+
 extern "C" int gbsym_tri_solve_b(gbsym_tri t, const double *b, double *x, void *stream) {
   if (!t || (t->n && (!x || !b))) return GBSYM_ERR_NULL_ARG;
   return guarded([&] {
@@ -762,7 +772,7 @@ extern "C" int gbsym_tri_solve_host(gbsym_tri t, double *x, int k, int layout) {
         // in place over the CPU-GPU link: the sync-free sweep reads each
         // right-hand side once and writes each result once, and rows
         // exchange values through its device scratch, never through x
-        run_syncfree<double>(t, static_cast<double *>(dp), k, s);
+        run_syncfree<double>(t, static_cast<double *>(dp), k, s, nullptr);
         const int code = tri_read_error(t, s);
         if (code) throw Err{code};
         return;

@@ -122,6 +122,9 @@ namespace gbsym {
 // selects the "redundant" row formula (k == 1, FP64 only).
 void tri_solve_rowmajor(gbsym_tri_s *t, void *x, const void *b, int k, int dtype,
                         cudaStream_t s);
+// Out of place on device memory, row-major n x k: x = L^-1 b, b unchanged
+// (b and x must not overlap).
+void tri_solve_into(gbsym_tri_s *t, const void *b, void *x, int k, int dtype, cudaStream_t s);
 // Executor selection (exec.cu).
 void choose_exec(gbsym_tri_s *t);
 int effective_exec(const gbsym_tri_s *t, int k, bool redundant);

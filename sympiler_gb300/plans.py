@@ -149,6 +149,16 @@ class TriPlan:
         del torch
         return x
 
+    def solve_into(self, b, x, stream=None):
+        """x = L^-1 b on CUDA tensors of shape (n,) or (n, k) row-major; b
+        is left unchanged."""
+        k = 1 if b.dim() == 1 else b.shape[1]
+        if x.shape != b.shape or x.dtype != b.dtype:
+            raise TypeError("x must match b in shape and dtype")
+        check(lib().gbsym_tri_solve_into(self._h, _dev_ptr(b, None, "b"), _dev_ptr(x, None, "x"), int(k),
+                                         _dtype_code(b.dtype), _stream(stream)), "gbsym_tri_solve_into")
+        return x
+
     def solve_b(self, b, x, stream=None):
         torch = _torch()
         check(lib().gbsym_tri_solve_b(self._h, _dev_ptr(b, torch.float64, "b"),

@@ -468,3 +468,21 @@ def etree_lower_csr(n, Lp, Li):
     if st != 0:
         raise GbsymError(st, "etree_lower_csr")
     return parent[: int(n)]
+
+
+# ---- drop-in plan cache (no counterpart in the reference) ---------------------
+
+def dropin_cache(capacity):
+    """Let the drop-ins keep up to ``capacity`` plans, keyed by the arrays
+    they were given (0, the default, turns the cache off): see
+    gbsym_dropin_cache in include/gbsym.h.  Changing a cached matrix's arrays
+    in place requires a new :func:`dropin_cache_version`."""
+    st = lib().gbsym_dropin_cache(int(capacity))
+    if st != 0:
+        raise GbsymError(st, "dropin_cache")
+
+
+def dropin_cache_version(version):
+    """Declare that matrices passed before may have changed: plans cached
+    under another version are dropped."""
+    lib().gbsym_dropin_cache_version(int(version))

@@ -274,6 +274,39 @@ def test_syncfree_lane_layouts_fp32_fp64(gpu, orc, monkeypatch, w, alt):
                 assert np.array_equal(x.cpu().numpy(), ref), (w, dt, k, alt)
 
 
+@pytest.mark.parametrize("exec_mode", [1, 2, 4, 5])
+def test_out_of_place_solve_every_executor(gpu, orc, c2_factor, exec_mode):
+    """gbsym_tri_solve_into: x = L^-1 b with b unchanged, bit-identical to the
+    in-place solve and the oracle at 1, 8 and 64 right-hand sides in FP64,
+    and against the FP32 oracle in FP32."""
+    from sympiler_gb300.plans import TriPlan
+    _, L, _ = c2_factor
+    rng = np.random.default_rng(21)
+    plan = TriPlan(L.n, *L.astuple())
+    plan.set_exec(exec_mode)
+    for k in (1, 8, 64):
+        B = rng.standard_normal((L.n, k))
+        ref = _oracle_mrhs(orc, L, B)
+        b = torch.from_numpy(B.copy()).cuda()
+        x = torch.full_like(b, 7.0)
+        plan.solve_into(b if k > 1 else b.view(-1), x if k > 1 else x.view(-1))
+        plan.check()
+        assert np.array_equal(x.cpu().numpy(), ref), k
+        assert np.array_equal(b.cpu().numpy(), B), k
+    p32 = TriPlan(L.n, *L.astuple(), dtype="f32")
+    p32.set_exec(exec_mode)
+    B = rng.standard_normal((L.n, 4)).astype(np.float32)
+    b = torch.from_numpy(B.copy()).cuda()
+    x = torch.empty_like(b)
+    p32.solve_into(b, x)
+    p32.check()
+    got = x.cpu().numpy()
+    for c in range(4):
+        r = np.ascontiguousarray(B[:, c])
+        orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), r)
+        assert np.array_equal(got[:, c], r), c
+
+
 def test_autotune_picks_a_working_executor(gpu, orc, c2_factor):
     from sympiler_gb300.plans import TriPlan
     _, L, _ = c2_factor

@@ -207,3 +207,45 @@ def test_empty_system(gpu):
     sym_lib.sptrsv_csr(0, np.zeros(1, dtype=np.int32), np.zeros(0, dtype=np.int32), np.zeros(0), x)
     nl, lp, ls = sym_lib.build_levelset_csr(0, np.zeros(1, dtype=np.int32), np.zeros(0, dtype=np.int32))
     assert nl == 0 and list(lp) == [0] and len(ls) == 0
+
+
+def test_dropin_plan_cache(gpu, orc):
+    """With the drop-in plan cache on, a second sptrsv_csr / sptrsv_csc call
+    on the same arrays reuses the plan (fewer kernel launches: no level-set
+    build, no packing) and stays bit-exact; a new caller version drops the
+    plans, so values changed in place are picked up."""
+    from sympiler_gb300 import sym_lib
+    from sympiler_gb300.plans import kernel_launches
+    L = mg.tril(mg.lap2d(80))
+    Lt = mg.transpose(L)  # CSC of L
+    rng = np.random.default_rng(31)
+    sym_lib.dropin_cache(4)
+    try:
+        counts = []
+        for call in range(3):
+            b = rng.uniform(-1, 1, L.n)
+            want = b.copy()
+            orc.sptrsv_csr(L.n, *L.astuple(), want)
+            x = b.copy()
+            k0 = kernel_launches()
+            sym_lib.sptrsv_csr(L.n, L.p, L.i, L.x, x)
+            counts.append(kernel_launches() - k0)
+            assert np.array_equal(x, want), call
+            xc = b.copy()
+            sym_lib.sptrsv_csc(L.n, Lt.p, Lt.i, Lt.x, xc)
+            assert np.array_equal(xc, want), call
+        assert counts[1] < counts[0] and counts[2] == counts[1], counts
+        # values changed in place, announced by a new version
+        L.x[L.p[1:] - 1] *= 2.0
+        sym_lib.dropin_cache_version(1)
+        b = rng.uniform(-1, 1, L.n)
+        want = b.copy()
+        orc.sptrsv_csr(L.n, *L.astuple(), want)
+        x = b.copy()
+        k0 = kernel_launches()
+        sym_lib.sptrsv_csr(L.n, L.p, L.i, L.x, x)
+        assert kernel_launches() - k0 > counts[1]  # rebuilt
+        assert np.array_equal(x, want)
+    finally:
+        sym_lib.dropin_cache(0)
+        sym_lib.dropin_cache_version(0)
