@@ -1017,6 +1017,53 @@ def main():
         ex["autotuned"] = {"k1": EXEC_NAMES.get(plan.autotune(k=1)),
                            "k%d" % k: EXEC_NAMES.get(plan.autotune(k=k))}
         extras["executors"] = ex
+        # the reference-facing drop-in per call (host arrays: upload, level
+        # set, packing, solve, download), with the plan cache off and on,
+        # beside a plan build alone and the host LBC inspector
+        from sympiler_gb300 import sym_lib
+        xb = B[:, 0].cpu().numpy()
+
+        def dropin_once():
+            xh = xb.copy()
+            sym_lib.sptrsv_csr(L.n, L.p, L.i, L.x, xh)
+
+        def wall_median(fn, reps=5):
+            fn()
+            ts = []
+            for _ in range(reps):
+                t0 = time.perf_counter()
+                fn()
+                ts.append(time.perf_counter() - t0)
+            return statistics.median(ts)
+        t_drop = wall_median(dropin_once)
+        sym_lib.dropin_cache(2)
+        t_drop_cached = wall_median(dropin_once)
+        sym_lib.dropin_cache(0)
+
+        def build_plan():
+            TriPlan(L.n, *L.astuple())
+            torch.cuda.synchronize()
+        t_build = wall_median(build_plan, 3)
+        t_lbc = wall_median(lambda: sym_lib.get_coarse_levelSet_DAG_CSC_tree(L.n, L.p, L.i, 0, 16, -1, 4000), 3)
+        Cl = mg.tril(mg.convdiff3d(96))
+        t_lbc_c3 = wall_median(lambda: sym_lib.get_coarse_levelSet_DAG_CSC_tree(Cl.n, Cl.p, Cl.i, 0, 16, -1, 4000),
+                               3)
+
+        def build_plan_c3():
+            TriPlan(Cl.n, *Cl.astuple())
+            torch.cuda.synchronize()
+        t_build_c3 = wall_median(build_plan_c3, 3)
+        extras["dropin_sptrsv_csr_c2"] = {
+            "per_call_ms": t_drop * 1e3, "per_call_cached_ms": t_drop_cached * 1e3,
+            "note": "sym_lib.sptrsv_csr on host arrays, one right-hand side; cached: gbsym_dropin_cache(2), "
+                    "the plan built by the first call reused"}
+        extras["inspectors"] = {
+            "c2": {"plan_build_ms": t_build * 1e3, "lbc_host_ms": t_lbc * 1e3, "n": L.n},
+            "c3_lower": {"plan_build_ms": t_build_c3 * 1e3, "lbc_host_ms": t_lbc_c3 * 1e3, "n": Cl.n},
+            "note": "plan build = upload + GPU validation + GPU level set + packing (gbsym_tri_create from host "
+                    "arrays); LBC = the host DAG LBC inspector (get_coarse_levelSet_DAG_CSC_tree's role, 16 "
+                    "parts per coarse level, min level distance -1, division rate 4000)"}
+        del Cl
         # the same factor in FP32 with 64 right-hand sides
         extras["sptrsv_64rhs_fp32_c2"] = fp32_mrhs(L, dev, stream, flush, 64)
         # in place (gbsym_tri_solve) beside the out-of-place headline step

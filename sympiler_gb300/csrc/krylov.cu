@@ -9,8 +9,12 @@
 // GMRES follows pmgmres_ldlt_cr (sparse_blas/parsy/gmres/mgmres.cpp:
 // 839-987): modified Gram-Schmidt Arnoldi, the re-orthogonalisation test
 // (av + delta*h == av, delta = 1e-3), Givens rotations and back
-// substitution on the small Hessenberg matrix (kept on the host), stop on
-// |g[k+1]| <= tol * ||r0||.  It differs in two chosen ways: the system
+// substitution on the small Hessenberg matrix, stop on |g[k+1]| <= tol *
+// ||r0||.  All of it runs on the device: each Gram-Schmidt round is one
+// cooperative launch, the Hessenberg column, the re-orthogonalisation
+// decision, the rotations and the back substitution are single-thread
+// kernels, and the host reads each step's residual estimate one step late
+// (gmres() below).  It differs in two chosen ways: the system
 // product is a general CSR SpMV (the nonsymmetric operator), and the ILU0
 // preconditioner (lus_cr, mgmres.cpp:598-689) is applied on the right, in
 // FP32 or FP64 as the factor plans store it.  All vector work is FP64.
@@ -213,68 +217,113 @@ __global__ void k_scale(long long n, double alpha, const double *__restrict__ u,
     v[i] = alpha * u[i];
 }
 
-// The sum of m block partials, as k_reduce_final forms it (same threads,
-// same order), by the block that arrives last: every block publishes its
-// partials, then takes a ticket; the block holding the last ticket reads
-// them back through L2, stores the sums and resets the ticket for the next
-// launch.  One launch instead of three, the same bits.
-__device__ __forceinline__ void last_block_sums(int m, const double *pdot, double *out_dot, const double *pnorm,
-                                                double *out_norm, unsigned *ticket, double *sh) {
-  __shared__ bool last;
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  if (out_dot) {
-    double t = 0.0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) t += __ldcg(pdot + i);
-    t = block_sum(t, sh);
-    if (threadIdx.x == 0) out_dot[0] = t;
-  }
-  if (out_norm) {
-    double t = 0.0;
-    for (int i = threadIdx.x; i < m; i += blockDim.x) t += __ldcg(pnorm + i);
-    t = block_sum(t, sh);
-    if (threadIdx.x == 0) out_norm[0] = t;
-  }
-  if (threadIdx.x == 0) *ticket = 0;
+// ---- one whole Gram-Schmidt round in one cooperative launch --------------
+// The passes of a round depend on each other only through their dot
+// products, so instead of one launch per pass (and a kernel boundary
+// between passes) one launch runs them all: after a pass every block
+// publishes its partial sums, meets the others at a grid barrier, and sums
+// all partials itself in the same fixed order as k_reduce_final (so every
+// block holds the same bits).  Partials alternate between two buffers, so a block
+// that runs ahead into pass j+1 never overwrites a partial a slower block
+// still reads for pass j (all blocks have read pass j's before any can
+// pass barrier j+1).
+__device__ __forceinline__ unsigned ld_acquire_b32(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
 }
 
-// One fused modified Gram-Schmidt pass over v, its reductions finished in
-// the same launch:
-//   if vprev: v -= h[jprev] * vprev  (the previous projection)
-//   *out_dot  = v . vnext            (the next projection), if out_dot
-//   *out_norm = v . v                (if out_norm)
-__global__ void __launch_bounds__(kRedThreads)
-k_mgs_pass_sum(long long n, double *__restrict__ v, const double *__restrict__ vprev,
-               const double *__restrict__ hprev, const double *__restrict__ vnext, double *__restrict__ pdot,
-               double *__restrict__ pnorm, double *out_dot, double *out_norm, unsigned *ticket,
-               const int *__restrict__ run_if) {
-  __shared__ double sh[32];
-  if (run_if && *run_if == 0) return;  // a re-orthogonalisation pass that is not needed
-  const double h = vprev ? *hprev : 0.0;
-  double sd = 0.0, sn = 0.0;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-       i += (long long)gridDim.x * blockDim.x) {
-    double vi = v[i];
-    if (vprev) {
-      vi = vi - h * vprev[i];
-      v[i] = vi;
+// Bounded grid barrier on a counter that only grows (wrap-around compare);
+// false (and GBSYM_ERR_TIMEOUT in err) when the wait ran out.
+__device__ __forceinline__ bool gs_barrier(unsigned *bar, unsigned target, int *err) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    atomicAdd(bar, 1u);
+    int ok = 1;
+    long long it = 0;
+    const unsigned long long t0 = globaltimer_ns();
+    while ((int)(ld_acquire_b32(bar) - target) < 0) {
+      ++it;
+      if (it > kWaitLimitIters || ((it & 255) == 0 && globaltimer_ns() - t0 > kWaitLimitNs) ||
+          ((it & 255) == 0 && ld_relaxed(err) != 0)) {
+        atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
+        ok = 0;
+        break;
+      }
     }
-    if (vnext) sd += vi * vnext[i];
-    sn += vi * vi;
+    s_ok = ok;
   }
-  if (out_dot) {
-    sd = block_sum(sd, sh);
-    if (threadIdx.x == 0) pdot[blockIdx.x] = sd;
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// The sum of m partials in k_reduce_final's order, broadcast to the block.
+__device__ __forceinline__ double all_sum(int m, const double *p, double *sh, double *bcast) {
+  double t = 0.0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) t += __ldcg(p + i);
+  t = block_sum(t, sh);
+  if (threadIdx.x == 0) *bcast = t;
+  __syncthreads();
+  t = *bcast;
+  __syncthreads();
+  return t;
+}
+
+// Round of Arnoldi step k over v = V_{k+1} (V's columns ld apart):
+// pass j = 0..k applies projection j-1 (with the dot of pass j-1) and
+// takes the dot with V_j into sc[j]; pass k+1 applies projection k and
+// takes ||v||^2 into sc[k+1].  The first round also stores ||v||^2 before
+// any projection into sc[mr+1].  A second round (re-orthogonalisation)
+// runs only when *run_if is set; otherwise block 0 advances the barrier
+// counter by the arrivals the round would have made, and all return.
+__global__ void __launch_bounds__(kRedThreads)
+k_mgs_round(long long n, double *V, long long ld, int k, int mr, double *sc, int second,
+            const int *run_if, double *part, unsigned *bar, unsigned base, int *err) {
+  __shared__ double sh[32];
+  __shared__ double bc;
+  if (run_if && *run_if == 0) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(bar, (unsigned)(k + 2) * gridDim.x);
+    return;
   }
-  if (out_norm) {
-    sn = block_sum(sn, sh);
-    if (threadIdx.x == 0) pnorm[blockIdx.x] = sn;
+  double *v = V + (size_t)(k + 1) * ld;
+  const int m = gridDim.x;
+  double h = 0.0;
+  for (int j = 0; j <= k + 1; ++j) {
+    const double *vprev = j > 0 ? V + (size_t)(j - 1) * ld : nullptr;
+    const double *vnext = j <= k ? V + (size_t)j * ld : nullptr;
+    const bool want_norm = second ? j == k + 1 : (j == 0 || j == k + 1);
+    double sd = 0.0, sn = 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+      double vi = v[i];
+      if (vprev) {
+        vi = vi - h * vprev[i];
+        v[i] = vi;
+      }
+      if (vnext) sd += vi * vnext[i];
+      sn += vi * vi;
+    }
+    double *pd = part + (size_t)(j & 1) * 2 * m, *pn = pd + m;
+    if (vnext) {
+      sd = block_sum(sd, sh);
+      if (threadIdx.x == 0) pd[blockIdx.x] = sd;
+    }
+    if (want_norm) {
+      sn = block_sum(sn, sh);
+      if (threadIdx.x == 0) pn[blockIdx.x] = sn;
+    }
+    if (!gs_barrier(bar, base + (unsigned)(j + 1) * m, err)) return;
+    if (vnext) {
+      h = all_sum(m, pd, sh, &bc);
+      if (blockIdx.x == 0 && threadIdx.x == 0) sc[j] = h;
+    }
+    if (want_norm) {
+      const double t = all_sum(m, pn, sh, &bc);
+      if (blockIdx.x == 0 && threadIdx.x == 0) sc[second || j == k + 1 ? k + 1 : mr + 1] = t;
+    }
   }
-  last_block_sums(gridDim.x, pdot, out_dot, pnorm, out_norm, ticket, sh);
 }
 
 // v = alpha[0] * v, alpha read on the device
@@ -432,14 +481,9 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
   DBuf<double> V((size_t)(mr + 1) * n), r(n), w(n), sc(2 * (mr + 2));
   DBuf<double> st_buf((size_t)(mr + 1) * mr + 4 * (mr + 1) + GW_COUNT);
   DBuf<int> reorth(1);
-  DBuf<double> pd, pn;
-  DBuf<unsigned> ticket(1);
   Reducer red;
   Precond M{Lu, U, {}};
   const int blocks = red_blocks(n);
-  pd.alloc(blocks);
-  pn.alloc(blocks);
-  GB_CUDA(cudaMemsetAsync(ticket.p, 0, sizeof(unsigned), s));
   GmresState st;
   st.H = st_buf.p;
   st.c = st.H + (size_t)(mr + 1) * mr;
@@ -478,19 +522,30 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
   // takes the norm.  First round: sc[j] <- h[j][k], sc[k+1] <- ||v||^2,
   // sc[mr+1] <- ||v||^2 before orthogonalisation (av).  Second round (only
   // if k_gm_column set the flag): the same without av.
+  // the round's passes run in one cooperative launch (k_mgs_round); its
+  // grid barrier counts arrivals on gbar, whose expected value the host
+  // tracks in `base`
+  int rs_per_sm = 0;
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rs_per_sm, k_mgs_round, kRedThreads, 0));
+  GB_CHECK(rs_per_sm >= 1, GBSYM_ERR_UNSUPPORTED);
+  const int rblocks = std::max(1, std::min(blocks, rs_per_sm * num_sms()));
+  DBuf<double> part(4 * (size_t)rblocks);
+  DBuf<unsigned> gbar(1);
+  DBuf<int> gerr(1);
+  GB_CUDA(cudaMemsetAsync(gbar.p, 0, sizeof(unsigned), s));
+  GB_CUDA(cudaMemsetAsync(gerr.p, 0, sizeof(int), s));
+  unsigned base = 0;
   auto mgs_round = [&](int k, bool second) {
-    double *v = Vj(k + 1);
-    for (int j = 0; j <= k + 1; ++j) {
-      const double *vprev = j > 0 ? Vj(j - 1) : nullptr;
-      const double *vnext = j <= k ? Vj(j) : nullptr;
-      double *norm = nullptr;
-      if (!second && (j == 0 || j == k + 1)) norm = sc.p + (j == 0 ? mr + 1 : k + 1);
-      if (second && j == k + 1) norm = sc.p + k + 1;
-      k_mgs_pass_sum<<<blocks, kRedThreads, 0, s>>>(n, v, vprev, sc.p + (j > 0 ? j - 1 : 0), vnext, pd.p, pn.p,
-                                                    vnext ? sc.p + j : nullptr, norm, ticket.p,
-                                                    second ? reorth.p : nullptr);
-      check_launch();
-    }
+    long long nn = n, ld = n;
+    double *Vp = V.p, *scp = sc.p, *partp = part.p;
+    int kk = k, mrr = mr, sec = second ? 1 : 0;
+    const int *run_if = second ? reorth.p : nullptr;
+    unsigned *barp = gbar.p;
+    int *errp = gerr.p;
+    void *args[] = {&nn, &Vp, &ld, &kk, &mrr, &scp, &sec, &run_if, &partp, &barp, &base, &errp};
+    GB_CUDA(cudaLaunchCooperativeKernel((const void *)k_mgs_round, dim3(rblocks), dim3(kRedThreads), args, 0, s));
+    check_launch();
+    base += (unsigned)(k + 2) * rblocks;
   };
   for (int itr = 0; itr < maxit && !converged && !breakdown; ++itr) {
     csr_spmv(A, x, r.p, GBSYM_F64, s);
@@ -564,7 +619,10 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
   check_launch();
   red.dot(n, r.p, r.p, sc.p, 0, nullptr, s);
   GB_CUDA(cudaMemcpyAsync(hs, sc.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+  int werr = 0;
+  GB_CUDA(cudaMemcpyAsync(&werr, gerr.p, sizeof(int), cudaMemcpyDeviceToHost, s));
   GB_CUDA(cudaStreamSynchronize(s));
+  if (werr) throw Err{werr};  // a Gram-Schmidt barrier gave up
   if (res) {
     res->iterations = itr_used;
     res->restarts = restarts;
