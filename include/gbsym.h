@@ -465,11 +465,11 @@ int gbsym_tri_solve(gbsym_tri t, void *x, int k, int layout, int dtype,
 /* Out of place on device memory: x = L^-1 b for k row-major right-hand
  * sides (n x k, dtype matching the plan's value storage); b is left
  * unchanged and must not overlap x (b == x solves in place).  The results
- * are bit-identical to gbsym_tri_solve's.  The sync-free executor reads b
- * and publishes each result straight into x, so it writes the solution
- * once instead of twice; a solution value whose bits are all ones (a NaN
- * carried from a NaN input) is stored as the default NaN.  The other
- * executors copy b into x and solve in place.  Stream-ordered. */
+ * are bit-identical to gbsym_tri_solve's.  With k >= 32 the sync-free
+ * executor reads b and publishes each result straight into x, so it writes
+ * the solution once instead of twice; a solution value whose bits are all
+ * ones (a NaN carried from a NaN input) is then stored as the default NaN.
+ * Otherwise b is copied into x and solved in place.  Stream-ordered. */
 int gbsym_tri_solve_into(gbsym_tri t, const void *b, void *x, int k, int dtype,
                          void *stream);
 /* The lbc_redundant row formula: x_i = ((0 - sum_j L_ij x_j) + b_i)/L_ii. */

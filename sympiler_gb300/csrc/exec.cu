@@ -102,8 +102,14 @@ void tri_solve_rowmajor(gbsym_tri_s *t, void *x, const void *b, int k, int dtype
 void tri_solve_into(gbsym_tri_s *t, const void *b, void *x, int k, int dtype, cudaStream_t s) {
   if (t->n == 0 || k == 0) return;
   GB_CHECK((dtype == GBSYM_F64) == (t->vdtype == GBSYM_F64), GBSYM_ERR_UNSUPPORTED);
-  if (effective_exec(t, k, false) == GBSYM_EXEC_SYNCFREE) {
-    // the sweep reads b and publishes each result straight into x
+  // With many right-hand sides the sweep reads b and publishes each result
+  // straight into x (one write of the solution instead of two; C2 factor,
+  // 64 RHS: 299 MB of DRAM traffic per solve against 407 MB).  With few,
+  // a row's values are too short for that to matter and the in-place
+  // sweep's scratch in packed row order, whose runs are contiguous, is
+  // faster (C2 factor, one RHS: 236 us publishing into x against 212 us
+  // for the copy and the in-place solve).
+  if (k >= 32 && effective_exec(t, k, false) == GBSYM_EXEC_SYNCFREE) {
     if (dtype == GBSYM_F64) run_syncfree<double>(t, (double *)x, k, s, (const double *)b);
     else run_syncfree<float>(t, (float *)x, k, s, (const float *)b);
     return;

@@ -228,6 +228,12 @@ template <>
 inline TriView<double> view_of<double>(const gbsym_tri_s *t) { return t->view64(); }
 template <>
 inline TriView<float> view_of<float>(const gbsym_tri_s *t) { return t->view32(); }
+template <class T>
+inline TriView<T> view_packed_of(const gbsym_tri_s *t);
+template <>
+inline TriView<double> view_packed_of<double>(const gbsym_tri_s *t) { return t->view64_packed(); }
+template <>
+inline TriView<float> view_packed_of<float>(const gbsym_tri_s *t) { return t->view32_packed(); }
 
 // Host entry points of the executors (one translation unit each).
 template <class T>

@@ -142,7 +142,9 @@ __global__ void __launch_bounds__(kSfBlock, KS <= 4 ? 3 : 2)
 k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ unit_row,
            const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
   // in place (b null): right-hand sides from x, results to x and published
-  // to y; out of place: right-hand sides from b, results published to y = x
+  // to y, the plan's scratch, in packed row order (A's dependency columns
+  // are then packed row numbers); out of place: right-hand sides from b,
+  // results published to y = x in the caller's row order
   const T *rhs = b ? b : x;
   const bool store_x = y != x;
   constexpr unsigned FULL = 0xffffffffu;
@@ -276,7 +278,7 @@ k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ 
           out[w] = not_sentinel(acc[w]);
         }
         if (store_x) vstore<T, VEC>(x + (size_t)rs.orig * k + r, acc);
-        st_rlx<T, VEC>(y + (size_t)rs.orig * k + r, out);
+        st_rlx<T, VEC>(y + (size_t)(store_x ? row : rs.orig) * k + r, out);
       }
     }
   }
@@ -306,7 +308,7 @@ static void launch_coop(gbsym_tri_s *t, int k_of_launch, K kernel, cudaStream_t 
 // every round (C2 64-RHS: 500 us at KS = 4 against 416 us at KS = 3).
 template <class T, int G, int AR, int KS, bool OV>
 static void sf_gk(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s) {
-  const TriView<T> A = view_of<T>(t);
+  const TriView<T> A = y != x ? view_packed_of<T>(t) : view_of<T>(t);
   const Units U = sf_units(t, 32 / G);
   // FP64 takes one value per lane: the polling then keeps two rounds of
   // loads in flight, which outweighs the narrower loads (measured 6-25%

@@ -433,6 +433,51 @@ static void pack_values(gbsym_tri_s *t, const int *d_p, const int *d_i, const do
   check_launch();
 }
 
+// Dependency columns in packed-row numbering, for the sync-free sweep's
+// scratch copy of the solution, which it keeps in packed (level) order: a
+// warp unit then publishes its rows into one contiguous run, and the
+// dependencies of consecutive rows of a level, which are mostly
+// consecutive rows of earlier levels, are read in runs too.  Slots past a
+// row's length are never read; they are set to 0.
+__global__ void k_inverse_perm(int n, const int *__restrict__ perm, int *__restrict__ inv) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) inv[perm[k]] = k;
+}
+__global__ void k_packed_slab_cols(int n, int K, int npad, const int *__restrict__ len,
+                                   const int *__restrict__ sci, const int *__restrict__ inv, int *__restrict__ scp) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+    for (int q = 0; q < K; ++q) {
+      const size_t at = (size_t)q * npad + k;
+      scp[at] = q < len[k] ? inv[sci[at]] : 0;
+    }
+}
+__global__ void k_packed_ov_cols(long long m, const int *__restrict__ oci, const int *__restrict__ inv,
+                                 int *__restrict__ ocp) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
+       e += (long long)gridDim.x * blockDim.x)
+    ocp[e] = inv[oci[e]];
+}
+
+static void build_packed_cols(gbsym_tri_s *t, cudaStream_t s) {
+  const int n = t->n;
+  t->scp.alloc((size_t)t->K * t->npad);
+  t->ocp.alloc(t->nov);
+  if (!n) return;
+  DBuf<int> inv(n);
+  const int g = std::max(1, std::min(div_up(n, 256), num_sms() * 8));
+  k_inverse_perm<<<g, 256, 0, s>>>(n, t->perm.p, inv.p);
+  check_launch();
+  if (t->K) {
+    k_packed_slab_cols<<<g, 256, 0, s>>>(n, t->K, t->npad, t->len.p, t->sci.p, inv.p, t->scp.p);
+    check_launch();
+  }
+  if (t->nov) {
+    k_packed_ov_cols<<<std::max(1, std::min(div_up(t->nov, 256), num_sms() * 8)), 256, 0, s>>>(
+        t->nov, t->oci.p, inv.p, t->ocp.p);
+    check_launch();
+  }
+  GB_CUDA(cudaStreamSynchronize(s));  // inv is freed on return
+}
+
 // ---------------------------------------------------------------------------
 // plan construction
 gbsym_tri_s *tri_build(int n, const int *d_p, const int *d_i, const double *d_x,
@@ -514,6 +559,7 @@ gbsym_tri_s *tri_build(int n, const int *d_p, const int *d_i, const double *d_x,
     for (int v : lens) nnz_off += v;
   }
   t->nnz_off = nnz_off;
+  build_packed_cols(t.get(), s);
   t->bar.alloc(1);
   GB_CUDA(cudaMemsetAsync(t->bar.p, 0, sizeof(unsigned), s));
   choose_exec(t.get());

@@ -78,6 +78,7 @@ struct gbsym_tri_s {
   int K = 0, npad = 0;               // slab width and stride
   long long nov = 0;                 // overflow entries
   gbsym::DBuf<int> lev_ptr, perm, len, sci, ovp, oci;
+  gbsym::DBuf<int> scp, ocp;         // sci / oci in packed-row numbering (sync-free scratch order)
   gbsym::DBuf<double> sv64, ov64, dg64, rc64;
   gbsym::DBuf<float> sv32, ov32, dg32, rc32;
   int arith = GBSYM_ARITH_EXACT;      // GBSYM_ARITH_EXACT or GBSYM_ARITH_FUSED
@@ -113,6 +114,19 @@ struct gbsym_tri_s {
   gbsym::TriView<float> view32() const {
     return {K, npad, perm.p, len.p, sci.p, sv32.p, nov ? ovp.p : nullptr, oci.p, ov32.p,
             kind == GBSYM_ILU_UNIT_LOWER ? nullptr : dg32.p, rc32.p};
+  }
+  // The same views with dependency columns in packed-row numbering.
+  gbsym::TriView<double> view64_packed() const {
+    gbsym::TriView<double> v = view64();
+    v.sci = scp.p;
+    v.oci = ocp.p;
+    return v;
+  }
+  gbsym::TriView<float> view32_packed() const {
+    gbsym::TriView<float> v = view32();
+    v.sci = scp.p;
+    v.oci = ocp.p;
+    return v;
   }
   ~gbsym_tri_s();
 };
