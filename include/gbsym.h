@@ -29,10 +29,10 @@
  *
  * Floating point: every row of every solve and product is accumulated in
  * the reference's storage order with separately rounded multiply and
- * subtract (no fused multiply-add), so FP64 results are bit-identical to
- * the reference compiled without floating-point contraction, for rows with
- * at most GBSYM_EXACT_ROW_MAX off-diagonal entries.  Longer rows use
- * warp-cooperative partial sums (relative difference ~1e-15).
+ * subtract (no fused multiply-add) and a correctly rounded division, so
+ * FP64 results are bit-identical to the reference compiled without
+ * floating-point contraction, whatever the row lengths.  The opt-in fused
+ * arithmetic of gbsym_tri_set_arith is the one exception.
  */
 #ifndef GBSYM_H
 #define GBSYM_H
@@ -56,8 +56,6 @@ enum gbsym_status {
   GBSYM_ERR_NOT_CONVERGED = 8, /* Krylov driver hit its iteration limit    */
   GBSYM_ERR_UNSUPPORTED = 9    /* option combination not implemented       */
 };
-
-#define GBSYM_EXACT_ROW_MAX 4096
 
 /* Status of the most recent drop-in call on this host thread. */
 int gbsym_last_error(void);
