@@ -141,7 +141,8 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   // (executor, parameter) candidates: the sync-free sweep is tried at one,
   // two and three blocks per SM (parameter bits 0-2) and, for several
   // right-hand sides, with its other lane layout (bit 3: two values per
-  // lane in FP64, one in FP32); the partitioned executor (k = 1 only) at
+  // lane in FP64 instead of one, two in FP32 instead of four); the
+  // partitioned executor (k = 1 only) at
   // several partition sizes
   std::vector<std::pair<int, int>> cands = {{GBSYM_EXEC_LEVELSET, 0}, {GBSYM_EXEC_PERSISTENT, 0},
                                             {GBSYM_EXEC_SYNCFREE, 1}, {GBSYM_EXEC_SYNCFREE, 2},

@@ -314,10 +314,14 @@ static void sf_gk(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s)
   // loads in flight, which outweighs the narrower loads (measured 6-25%
   // faster for 8 to 64 right-hand sides on the C2 factor).  FP32 keeps
   // 2- or 4-wide lanes by default, which measured faster there for 8 and
-  // 64; the autotuner may choose one value per lane (sf_alt_lanes).
+  // 64; the autotuner may choose two values per lane (sf_alt_lanes), which
+  // halves the rows of a warp unit at 8 right-hand sides.
   if constexpr (sizeof(T) == 4) {
     if (k > 1 && t->sf_alt_lanes == 1) {
-      launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+      if (k % 2 == 0 && ((uintptr_t)x | (uintptr_t)(b ? b : x)) % 8 == 0)
+        launch_coop(t, k, k_syncfree<T, G, 2, AR, KS, OV ? ov_batch<T, 2>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+      else
+        launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
     if (k % 4 == 0 && ((uintptr_t)x | (uintptr_t)(b ? b : x)) % 16 == 0) {
@@ -348,12 +352,15 @@ static void sf_ar(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s)
   // 32 right-hand sides (C2: 8 RHS 260 -> 246 us, 32 RHS 325 -> 308 us
   // against half as many lanes, each taking two slices).  Which is faster
   // depends on the matrix (the C4 batch prefers half at 8 RHS), so the
-  // autotuner chooses (sf_alt_lanes).  FP32 lanes carry two or four values
-  // by default, one (as many lanes as FP64's default) as the alternative.
+  // autotuner chooses (sf_alt_lanes).  FP32 lanes carry four values (two
+  // when k is not a multiple of four) by default, two as the alternative.
   int g64 = 2;
   while (g64 < k && g64 < 32) g64 <<= 1;
+  int g32alt = 2;
+  while (g32alt * 2 < k && g32alt < 32) g32alt <<= 1;
   const bool alt = t->sf_alt_lanes == 1;
-  switch ((sizeof(T) == 8) != alt ? g64 : lanes_for(k, sizeof(T))) {
+  const int lanes = sizeof(T) == 8 ? (alt ? lanes_for(k, sizeof(T)) : g64) : (alt ? g32alt : lanes_for(k, sizeof(T)));
+  switch (lanes) {
     case 2: sf_gk<T, 2, AR, KS, OV>(t, x, y, b, k, s); break;
     case 4: sf_gk<T, 4, AR, KS, OV>(t, x, y, b, k, s); break;
     case 8: sf_gk<T, 8, AR, KS, OV>(t, x, y, b, k, s); break;

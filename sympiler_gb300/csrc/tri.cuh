@@ -93,7 +93,7 @@ struct gbsym_tri_s {
   int sf_blocks_per_sm = 0;          // sync-free grid, forced for every k (0: default)
   int sf_bps_tuned[2] = {0, 0};      // sync-free blocks per SM the autotuner chose, k = 1 and k > 1 (0: default)
   int sf_alt_lanes = 0;              // k > 1, 1: the other lane layout (FP64: two values per
-                                     // lane; FP32: one), the autotuner's choice
+                                     // lane; FP32: two), the autotuner's choice
   int sf_deal = 0;                   // sync-free unit dealing: SM count to spread over (0: plain order)
   struct PartPlan {
     int R = 0, nparts = 0, ngroups = 0;  // rows per partition (0: not built)

@@ -246,7 +246,8 @@ def test_syncfree_every_slab_width(gpu, orc, w):
 @pytest.mark.parametrize("w", [3, 5])
 def test_syncfree_lane_layouts_fp32_fp64(gpu, orc, monkeypatch, w, alt):
     """Both lane layouts of the multi-RHS sync-free sweep (FP64: one or two
-    values per lane; FP32: two/four or one), with and without rows past the
+    values per lane; FP32: four, or two when k is odd, or two), with and
+    without rows past the
     slab: FP64 bit-exact against the oracle, FP32 against the FP32 oracle
     column by column."""
     from sympiler_gb300._lib import EXEC_SYNCFREE
