@@ -67,7 +67,6 @@ void choose_exec(gbsym_tri_s *t) {
   if (const char *cb = std::getenv("GBSYM_CLUSTER_BLOCKS")) t->cluster_blocks = std::atoi(cb);
   if (const char *sb = std::getenv("GBSYM_SF_BLOCKS_PER_SM")) t->sf_blocks_per_sm = std::atoi(sb);
   if (const char *al = std::getenv("GBSYM_SF_ALT_LANES")) t->sf_alt_lanes = std::atoi(al) == 1;
-  if (const char *qu = std::getenv("GBSYM_SF_QUEUE")) t->sf_dynamic = std::atoi(qu) == 1;
   t->sf_deal = num_sms();
   if (const char *sd = std::getenv("GBSYM_SF_DEAL")) t->sf_deal = std::atoi(sd);
 }
@@ -140,12 +139,11 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   const long long m = (long long)t->n * k;
   DBuf<T> buf(m);
   // (executor, parameter) candidates: the sync-free sweep is tried at one,
-  // two and three blocks per SM (parameter bits 0-2); for several
-  // right-hand sides also with its other lane layout (bit 3: two values per
-  // lane in FP64 instead of one, two in FP32 instead of four).  The work
-  // queue (bit 4, GBSYM_SF_QUEUE) is not a candidate: it measured 1.5-2.3x
-  // slower than static dealing on every workload.  The partitioned executor
-  // (k = 1 only) is tried at several partition sizes.
+  // two and three blocks per SM (parameter bits 0-2) and, for several
+  // right-hand sides, with its other lane layout (bit 3: two values per
+  // lane in FP64 instead of one, two in FP32 instead of four); the
+  // partitioned executor (k = 1 only) at
+  // several partition sizes
   std::vector<std::pair<int, int>> cands = {{GBSYM_EXEC_LEVELSET, 0}, {GBSYM_EXEC_PERSISTENT, 0},
                                             {GBSYM_EXEC_SYNCFREE, 1}, {GBSYM_EXEC_SYNCFREE, 2},
                                             {GBSYM_EXEC_SYNCFREE, 3}, {GBSYM_EXEC_CLUSTER, 0}};
@@ -173,14 +171,13 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   float best_ms = 0;
   const int saved_rows = t->part_rows_pref;
   const int kk = k > 1 ? 1 : 0;
-  const int saved_bps = t->sf_bps_tuned[kk], saved_alt = t->sf_alt_lanes, saved_dyn = t->sf_dyn_tuned[kk];
+  const int saved_bps = t->sf_bps_tuned[kk], saved_alt = t->sf_alt_lanes;
   for (const auto &cand : cands) {
     const int e = cand.first;
     if (e == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = cand.second;
     if (e == GBSYM_EXEC_SYNCFREE) {
       t->sf_bps_tuned[kk] = cand.second & 7;
-      if (k > 1) t->sf_alt_lanes = (cand.second >> 3) & 1;
-      t->sf_dyn_tuned[kk] = (cand.second >> 4) & 1;
+      if (k > 1) t->sf_alt_lanes = cand.second >> 3;
     }
     std::vector<float> ms;
     for (int rep = 0; rep < 4; ++rep) {
@@ -209,13 +206,11 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   t->part_rows_pref = saved_rows;
   t->sf_bps_tuned[kk] = saved_bps;
   t->sf_alt_lanes = saved_alt;
-  t->sf_dyn_tuned[kk] = saved_dyn;
   if (best < 0) throw Err{GBSYM_ERR_TIMEOUT};
   if (best == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = best_rows;
   if (best == GBSYM_EXEC_SYNCFREE) {
     t->sf_bps_tuned[kk] = best_rows & 7;
-    if (k > 1) t->sf_alt_lanes = (best_rows >> 3) & 1;
-    t->sf_dyn_tuned[kk] = (best_rows >> 4) & 1;
+    if (k > 1) t->sf_alt_lanes = best_rows >> 3;
   }
   if (k == 1) t->exec = best; else t->exec_mrhs = best;
   std::lock_guard<std::mutex> lk(g_tuned_mu);

@@ -250,7 +250,7 @@ void part_launch(gbsym_tri_s *t, T *x, T *y, cudaStream_t s) {
 
 }  // namespace
 
-void fill_sentinel(void *y, size_t bytes, cudaStream_t s, unsigned *queue = nullptr);  // exec_syncfree.cu
+void fill_sentinel(void *y, size_t bytes, cudaStream_t s);  // exec_syncfree.cu
 
 template <class T>
 void run_part(gbsym_tri_s *t, T *x, cudaStream_t s) {

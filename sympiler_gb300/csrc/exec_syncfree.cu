@@ -33,23 +33,19 @@ Units sf_units(gbsym_tri_s *t, int rpw) {
 
 // Every published slot starts as the sentinel (all bits set): 16-byte
 // stores over the 16-byte multiple, 4-byte stores over the remainder.
-// (and, when queue is given, the sweep's work-queue counter starts at 0)
-__global__ void k_fill_sentinel(uint4 *__restrict__ p, size_t n16, unsigned *__restrict__ tail, int ntail,
-                                unsigned *queue) {
+__global__ void k_fill_sentinel(uint4 *__restrict__ p, size_t n16, unsigned *__restrict__ tail, int ntail) {
   const size_t stride = (size_t)gridDim.x * blockDim.x;
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n16; i += stride)
     p[i] = make_uint4(~0u, ~0u, ~0u, ~0u);
   if (blockIdx.x == 0 && (int)threadIdx.x < ntail) tail[threadIdx.x] = ~0u;
-  if (queue && blockIdx.x == 0 && threadIdx.x == 0) *queue = 0u;
 }
 
-void fill_sentinel(void *y, size_t bytes, cudaStream_t s, unsigned *queue) {
+void fill_sentinel(void *y, size_t bytes, cudaStream_t s) {
   const size_t n16 = bytes / 16;
   const int ntail = (int)((bytes - n16 * 16) / 4);
   const int grid = (int)std::max<size_t>(1, std::min<size_t>(div_up(n16, (size_t)256), (size_t)num_sms() * 8));
   k_fill_sentinel<<<grid, 256, 0, s>>>(reinterpret_cast<uint4 *>(y), n16,
-                                       reinterpret_cast<unsigned *>(static_cast<char *>(y) + n16 * 16), ntail,
-                                       queue);
+                                       reinterpret_cast<unsigned *>(static_cast<char *>(y) + n16 * 16), ntail);
   check_launch();
 }
 
@@ -61,8 +57,7 @@ void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s, const T *b) {
     t->sfy.reserve(bytes);
     y = reinterpret_cast<T *>(t->sfy.p);
   }
-  if (!t->sf_queue.p) t->sf_queue.alloc(1);
-  fill_sentinel(y, bytes, s, t->sf_queue.p);
+  fill_sentinel(y, bytes, s);
   const bool ov = t->nov > 0;
   switch (t->K) {
     case 0:

@@ -19,10 +19,6 @@ struct Units {
 
 Units sf_units(gbsym_tri_s *t, int rpw);
 
-// Sentinel fill of the sweep's published values; queue, when given, is the
-// work-queue counter of a dynamically scheduled sweep and is set to 0.
-void fill_sentinel(void *y, size_t bytes, cudaStream_t s, unsigned *queue = nullptr);
-
 // The sweep of a plan whose slab is at most KS entries wide (KS >= t->K),
 // into the sentinel-filled y; OV: the plan has rows longer than its slab.
 // In place (b null) y is the plan's scratch copy and x receives every value

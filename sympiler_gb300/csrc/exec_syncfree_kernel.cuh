@@ -102,9 +102,6 @@ __device__ __forceinline__ bool all_ready(const T (&v)[VEC]) {
 // timer); 2^32 cycles is about two seconds at this part's clocks.
 __device__ __forceinline__ long long clock_now() { return clock64(); }
 
-// Units a warp takes from the work queue at a time.
-constexpr int kSfChunk = 2;
-
 // Entries past the slab are polled and accumulated this many at a time:
 // one L2 round trip per group instead of one per entry (rows longer than
 // the slab otherwise wait a round trip per extra entry, twice).  Two for
@@ -143,7 +140,7 @@ __device__ __forceinline__ int deal_warp(int nsm) {
 template <class T, int G, int VEC, int AR, int KS, int OVB>
 __global__ void __launch_bounds__(kSfBlock, KS <= 4 ? 3 : 2)
 k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ unit_row,
-           const int *__restrict__ unit_cnt, int nunits, int nsm, int *err, unsigned *queue) {
+           const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
   // in place (b null): right-hand sides from x, results to x and published
   // to y, the plan's scratch, in packed row order (A's dependency columns
   // are then packed row numbers); out of place: right-hand sides from b,
@@ -157,25 +154,7 @@ k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ 
   const int warp = deal_warp(nsm);
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   const int nslices = (k + G * VEC - 1) / (G * VEC);
-  // Static dealing: warp w takes units w, w + W, w + 2W, ...  Work queue
-  // (queue non-null): a warp takes the next kSfChunk units from a global
-  // counter, asking for its next chunk as soon as it starts one, so the
-  // counter's round trip overlaps the work.  Either way every warp takes
-  // its units in increasing order, and a unit only waits on smaller ones,
-  // so the smallest unfinished unit always runs (a chunk asked for ahead
-  // is larger than every unit the warp still holds).
-  int u, chunk_end, next_chunk = 0;
-  if (queue) {
-    int t0 = 0;
-    if (lane == 0) t0 = (int)atomicAdd(queue, (unsigned)kSfChunk);
-    u = __shfl_sync(FULL, t0, 0);
-    chunk_end = u + kSfChunk;
-  } else {
-    u = warp;
-    chunk_end = nunits;
-  }
-  while (u < nunits) {
-    if (queue && u == chunk_end - kSfChunk && lane == 0) next_chunk = (int)atomicAdd(queue, (unsigned)kSfChunk);
+  for (int u = warp; u < nunits; u += nwarps) {
     const bool active = sub < unit_cnt[u];
     const int row = unit_row[u] + sub;
     RowStatic<T, KS> rs;
@@ -302,12 +281,6 @@ k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ 
         st_rlx<T, VEC>(y + (size_t)(store_x ? row : rs.orig) * k + r, out);
       }
     }
-    if (!queue) {
-      u += nwarps;
-    } else if (++u == chunk_end) {
-      u = __shfl_sync(FULL, next_chunk, 0);
-      chunk_end = u + kSfChunk;
-    }
   }
 }
 
@@ -333,17 +306,6 @@ static void launch_coop(gbsym_tri_s *t, int k_of_launch, K kernel, cudaStream_t 
 // unrolled slab loops match the plan's slab width issues no guard
 // instructions for slots a row cannot have, which the polling loop repeats
 // every round (C2 64-RHS: 500 us at KS = 4 against 416 us at KS = 3).
-// Whether the sweep takes its units from the work queue: forced by
-// sf_dynamic (GBSYM_SF_QUEUE=1 at plan creation), else static dealing.
-// The queue balances units whose latencies differ, but it gives up the
-// dealing that spreads each level over every SM, and on this part it
-// measured 1.5-2.3x slower on every workload (C2 1 and 64 RHS, the C3 ILU
-// apply, the C4 batch).
-inline bool sf_use_queue(const gbsym_tri_s *t, int k) {
-  if (t->sf_dynamic >= 0) return t->sf_dynamic != 0;
-  return t->sf_dyn_tuned[k > 1 ? 1 : 0] == 1;
-}
-
 template <class T, int G, int AR, int KS, bool OV>
 static void sf_gk(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s) {
   const TriView<T> A = y != x ? view_packed_of<T>(t) : view_of<T>(t);
@@ -357,26 +319,21 @@ static void sf_gk(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s)
   if constexpr (sizeof(T) == 4) {
     if (k > 1 && t->sf_alt_lanes == 1) {
       if (k % 2 == 0 && ((uintptr_t)x | (uintptr_t)(b ? b : x)) % 8 == 0)
-        launch_coop(t, k, k_syncfree<T, G, 2, AR, KS, OV ? ov_batch<T, 2>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p,
-                  sf_use_queue(t, k) ? t->sf_queue.p : (unsigned *)nullptr);
+        launch_coop(t, k, k_syncfree<T, G, 2, AR, KS, OV ? ov_batch<T, 2>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       else
-        launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p,
-                  sf_use_queue(t, k) ? t->sf_queue.p : (unsigned *)nullptr);
+        launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
     if (k % 4 == 0 && ((uintptr_t)x | (uintptr_t)(b ? b : x)) % 16 == 0) {
-      launch_coop(t, k, k_syncfree<T, G, 4, AR, KS, OV ? ov_batch<T, 4>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p,
-                  sf_use_queue(t, k) ? t->sf_queue.p : (unsigned *)nullptr);
+      launch_coop(t, k, k_syncfree<T, G, 4, AR, KS, OV ? ov_batch<T, 4>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
     if (k % 2 == 0 && ((uintptr_t)x | (uintptr_t)(b ? b : x)) % 8 == 0) {
-      launch_coop(t, k, k_syncfree<T, G, 2, AR, KS, OV ? ov_batch<T, 2>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p,
-                  sf_use_queue(t, k) ? t->sf_queue.p : (unsigned *)nullptr);
+      launch_coop(t, k, k_syncfree<T, G, 2, AR, KS, OV ? ov_batch<T, 2>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
       return;
     }
   }
-  launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p,
-                  sf_use_queue(t, k) ? t->sf_queue.p : (unsigned *)nullptr);
+  launch_coop(t, k, k_syncfree<T, G, 1, AR, KS, OV ? ov_batch<T, 1>() : 0>, s, A, x, y, b, k, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
 }
 
 template <class T, int AR, int KS, bool OV>

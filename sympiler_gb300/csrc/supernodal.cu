@@ -103,7 +103,7 @@ struct gbsym_sn_s {
 };
 
 namespace gbsym {
-void fill_sentinel(void *y, size_t bytes, cudaStream_t s, unsigned *queue = nullptr);  // exec_syncfree.cu
+void fill_sentinel(void *y, size_t bytes, cudaStream_t s);  // exec_syncfree.cu
 
 namespace {
 

@@ -95,9 +95,6 @@ struct gbsym_tri_s {
   int sf_alt_lanes = 0;              // k > 1, 1: the other lane layout (FP64: two values per
                                      // lane; FP32: two), the autotuner's choice
   int sf_deal = 0;                   // sync-free unit dealing: SM count to spread over (0: plain order)
-  int sf_dyn_tuned[2] = {0, 0};      // sync-free work queue (1) or static dealing (0), the autotuner's choice
-  int sf_dynamic = -1;               // forced work queue (1) / static dealing (0); -1: not forced
-  gbsym::DBuf<unsigned> sf_queue;    // the work queue's counter
   struct PartPlan {
     int R = 0, nparts = 0, ngroups = 0;  // rows per partition (0: not built)
     gbsym::DBuf<int> part_group, group_ptr, rows;

@@ -308,31 +308,6 @@ def test_out_of_place_solve_every_executor(gpu, orc, c2_factor, exec_mode):
         assert np.array_equal(got[:, c], r), c
 
 
-@pytest.mark.parametrize("k", [1, 64])
-def test_syncfree_work_queue(gpu, orc, c2_factor, monkeypatch, k):
-    """The sync-free sweep with its units taken from the global work queue
-    (GBSYM_SF_QUEUE=1) instead of dealt statically: bit-exact in place and
-    out of place."""
-    from sympiler_gb300._lib import EXEC_SYNCFREE
-    from sympiler_gb300.plans import TriPlan
-    monkeypatch.setenv("GBSYM_SF_QUEUE", "1")
-    _, L, _ = c2_factor
-    plan = TriPlan(L.n, *L.astuple())
-    plan.set_exec(EXEC_SYNCFREE)
-    B = np.random.default_rng(40 + k).standard_normal((L.n, k))
-    ref = _oracle_mrhs(orc, L, B)
-    for repeat in range(2):
-        x = torch.from_numpy(B.copy()).cuda()
-        plan.solve(x if k > 1 else x.view(-1))
-        plan.check()
-        assert np.array_equal(x.cpu().numpy(), ref), repeat
-    b = torch.from_numpy(B.copy()).cuda()
-    x = torch.empty_like(b)
-    plan.solve_into(b, x)
-    plan.check()
-    assert np.array_equal(x.cpu().numpy(), ref)
-
-
 def test_autotune_picks_a_working_executor(gpu, orc, c2_factor):
     from sympiler_gb300.plans import TriPlan
     _, L, _ = c2_factor
