@@ -202,3 +202,103 @@ def test_drop_ins_report_null_arrays_without_a_gpu(name, nint):
     for fn in (L.gbsym_ltsolve, L.gbsym_parsy_lsolve):
         assert fn(4, None, None, None, None) == 0
         assert L.gbsym_last_error() == _lib.ERR_NULL_ARG
+
+
+@pytest.mark.gpu
+def test_cpp_shim_runs_on_the_gpu(gpu, tmp_path):
+    """A caller written against the reference's sym_lib signatures, compiled
+    against include/gbsym_sym_lib.hpp and linked to libgbsym.so, solves on
+    the GPU: sptrsv_csr, sptrsv_csr_levelset with the level set from
+    build_levelSet_CSC, sptrsv_csc, ltsolve and spmv_csr on a 2D Laplacian,
+    each compared bit for bit inside the program with a plain serial loop in
+    the reference's operation order (compiled without contraction)."""
+    from sympiler_gb300 import _lib
+    src = tmp_path / "gpu_caller.cpp"
+    src.write_text(r'''
+#include "gbsym_sym_lib.hpp"
+#include <cstdio>
+#include <cstring>
+#include <vector>
+int main() {
+  const int g = 60, n = g * g;
+  std::vector<int> Lp(n + 1), Li;          // lower CSR of the 5-point Laplacian, diagonal last
+  std::vector<double> Lx;
+  std::vector<int> Ap(n + 1), Ai;          // full CSR
+  std::vector<double> Ax;
+  for (int i = 0; i < n; ++i) {
+    const int x = i % g, y = i / g;
+    if (y > 0) { Li.push_back(i - g); Lx.push_back(-1.0); }
+    if (x > 0) { Li.push_back(i - 1); Lx.push_back(-1.0); }
+    Li.push_back(i); Lx.push_back(4.0 + 0.01 * (i % 7));
+    Lp[i + 1] = (int)Li.size();
+    if (y > 0) { Ai.push_back(i - g); Ax.push_back(-1.0); }
+    if (x > 0) { Ai.push_back(i - 1); Ax.push_back(-1.0); }
+    Ai.push_back(i); Ax.push_back(4.0 + 0.01 * (i % 7));
+    if (x < g - 1) { Ai.push_back(i + 1); Ax.push_back(-1.0); }
+    if (y < g - 1) { Ai.push_back(i + g); Ax.push_back(-1.0); }
+    Ap[i + 1] = (int)Ai.size();
+  }
+  // CSC of L (diagonal first in each column) = upper CSR of L^T
+  std::vector<int> Cp(n + 1, 0), Ci(Li.size());
+  std::vector<double> Cx(Li.size());
+  for (int e = 0; e < (int)Li.size(); ++e) Cp[Li[e] + 1]++;
+  for (int j = 0; j < n; ++j) Cp[j + 1] += Cp[j];
+  std::vector<int> fill(Cp.begin(), Cp.end() - 1);
+  for (int i = 0; i < n; ++i)
+    for (int e = Lp[i]; e < Lp[i + 1]; ++e) { Ci[fill[Li[e]]] = i; Cx[fill[Li[e]]++] = Lx[e]; }
+  std::vector<double> b(n);
+  for (int i = 0; i < n; ++i) b[i] = ((i * 37) % 101) / 50.0 - 1.0;
+  // serial checks in the reference's order
+  std::vector<double> want(b);
+  for (int i = 0; i < n; ++i) {
+    double xi = want[i];
+    for (int e = Lp[i]; e < Lp[i + 1] - 1; ++e) xi -= Lx[e] * want[Li[e]];
+    want[i] = xi / Lx[Lp[i + 1] - 1];
+  }
+  std::vector<double> want_t(b);           // L^T x = b on the CSC of L
+  for (int j = n - 1; j >= 0; --j) {
+    double xj = want_t[j];
+    for (int e = Cp[j] + 1; e < Cp[j + 1]; ++e) xj -= Cx[e] * want_t[Ci[e]];
+    want_t[j] = xj / Cx[Cp[j]];
+  }
+  std::vector<double> want_y(n, 0.0);
+  for (int i = 0; i < n; ++i)
+    for (int e = Ap[i]; e < Ap[i + 1]; ++e) want_y[i] += Ax[e] * b[Ai[e]];
+  int bad = 0;
+  auto same = [&](const std::vector<double> &a, const std::vector<double> &c, const char *what) {
+    if (std::memcmp(a.data(), c.data(), a.size() * sizeof(double)) != 0) {
+      std::printf("%s differs\n", what);
+      ++bad;
+    }
+  };
+  std::vector<double> x(b);
+  sym_lib::sptrsv_csr(n, Lp.data(), Li.data(), Lx.data(), x.data());
+  same(x, want, "sptrsv_csr");
+  int *lptr = nullptr, *lset = nullptr;
+  const int levels = sym_lib::build_levelSet_CSC(n, Cp.data(), Ci.data(), lptr, lset);
+  x = b;
+  sym_lib::sptrsv_csr_levelset(n, Lp.data(), Li.data(), Lx.data(), x.data(), levels, lptr, lset);
+  same(x, want, "sptrsv_csr_levelset");
+  delete[] lptr;
+  delete[] lset;
+  x = b;
+  sym_lib::sptrsv_csc(n, Cp.data(), Ci.data(), Cx.data(), x.data());
+  same(x, want, "sptrsv_csc");
+  x = b;
+  if (sym_lib::ltsolve(n, Cp.data(), Ci.data(), Cx.data(), x.data()) != 1) ++bad;
+  same(x, want_t, "ltsolve");
+  std::vector<double> y(n, 0.0);
+  sym_lib::spmv_csr(n, Ap.data(), Ai.data(), Ax.data(), b.data(), y.data());
+  same(y, want_y, "spmv_csr");
+  std::printf("%s levels=%d\n", bad ? "FAILED" : "ok", levels);
+  return bad || gbsym_last_error() != 0;
+}
+''')
+    exe = tmp_path / "gpu_caller"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    r = subprocess.run(["g++", "-std=c++11", "-O2", "-ffp-contract=off", "-I" + os.path.join(ROOT, "include"),
+                        str(src), "-o", str(exe), "-L" + libdir, "-lgbsym", "-Wl,-rpath," + libdir],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0 and out.stdout.startswith("ok levels=119"), (out.stdout, out.stderr)
