@@ -453,3 +453,32 @@ def test_lower_csc_plan_matches_column_push_oracle(gpu, orc):
     P.solve(x)
     P.check()
     assert np.array_equal(x.cpu().numpy(), ref)
+
+
+@pytest.mark.parametrize("k", [1, 64])
+def test_syncfree_solve_captured_in_cuda_graph(gpu, orc, c2_factor, k):
+    """A plan's sync-free solve (sentinel fill + cooperative sweep) captured
+    into a CUDA graph and replayed on new right-hand sides: every replay
+    bit-exact.  The first, uncaptured solve allocates the plan's scratch and
+    warp units; replays allocate nothing."""
+    from sympiler_gb300._lib import EXEC_SYNCFREE
+    from sympiler_gb300.plans import TriPlan
+    _, L, _ = c2_factor
+    plan = TriPlan(L.n, *L.astuple())
+    plan.set_exec(EXEC_SYNCFREE)
+    X = torch.zeros((L.n, k), dtype=torch.float64, device="cuda")
+    Xv = X if k > 1 else X.view(-1)
+    plan.solve(Xv)  # warm: scratch and unit lists
+    torch.cuda.synchronize()
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        plan.solve(Xv)
+    rng = np.random.default_rng(60 + k)
+    for replay in range(3):
+        B = rng.standard_normal((L.n, k))
+        X.copy_(torch.from_numpy(B))
+        g.replay()
+        torch.cuda.synchronize()
+        plan.check()
+        assert np.array_equal(X.cpu().numpy(), _oracle_mrhs(orc, L, B)), replay
