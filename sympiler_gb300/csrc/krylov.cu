@@ -171,6 +171,9 @@ void pcg(gbsym_csr_s *A, gbsym_tri_s *L, gbsym_tri_s *Lt, const double *b, doubl
   const double bnorm = hs[S_BB] > 0 ? std::sqrt(hs[S_BB]) : 1.0;
   double rel = std::sqrt(hs[S_RR]) / bnorm;
   int it = 0;
+  cudaEvent_t rr_ready = nullptr;
+  GB_CUDA(cudaEventCreateWithFlags(&rr_ready, cudaEventDisableTiming));
+  std::unique_ptr<CUevent_st, void (*)(cudaEvent_t)> ev_guard(rr_ready, [](cudaEvent_t e) { cudaEventDestroy(e); });
   while (rel > tol && it < maxit) {
     csr_spmv(A, p.p, q.p, GBSYM_F64, s);
     // pq -> S_PQ, alpha = rz / pq -> S_ALPHA
@@ -180,10 +183,13 @@ void pcg(gbsym_csr_s *A, gbsym_tri_s *L, gbsym_tri_s *Lt, const double *b, doubl
     k_reduce_final<<<1, kRedThreads, 0, s>>>(red.blocks, red.partial.p, sc.p + S_RR, 0, nullptr);
     check_launch();
     GB_CUDA(cudaMemcpyAsync(hs + S_RR, sc.p + S_RR, sizeof(double), cudaMemcpyDeviceToHost, s));
-    // speculatively continue with the preconditioner while the norm travels
+    GB_CUDA(cudaEventRecord(rr_ready, s));
+    // continue with the preconditioner while the norm travels; the host
+    // waits only for the norm, so the GPU keeps working on the two sweeps
+    // while the host checks it and queues the rest of the iteration
     GB_CUDA(cudaMemcpyAsync(z.p, r.p, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
     apply_ic0(L, Lt, z.p, s);
-    GB_CUDA(cudaStreamSynchronize(s));
+    GB_CUDA(cudaEventSynchronize(rr_ready));
     ++it;
     rel = std::sqrt(hs[S_RR]) / bnorm;
     if (rel <= tol) break;
