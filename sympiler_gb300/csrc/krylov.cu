@@ -534,7 +534,10 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
   int rs_per_sm = 0;
   GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rs_per_sm, k_mgs_round, kRedThreads, 0));
   GB_CHECK(rs_per_sm >= 1, GBSYM_ERR_UNSUPPORTED);
-  const int rblocks = std::max(1, std::min(blocks, rs_per_sm * num_sms()));
+  // two blocks per SM: the round's grid barriers cost more with more blocks
+  // and its streaming needs enough of them (C3 GMRES, FP32 preconditioner:
+  // 0.1378 / 0.1258 / 0.1278 / 0.1353 s at 1 / 2 / 4 / 8 blocks per SM)
+  const int rblocks = std::max(1, std::min(blocks, std::min(rs_per_sm, 2) * num_sms()));
   DBuf<double> part(4 * (size_t)rblocks);
   DBuf<unsigned> gbar(1);
   DBuf<int> gerr(1);
