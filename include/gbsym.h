@@ -525,7 +525,8 @@ int gbsym_pcg(gbsym_csr A, gbsym_tri L, gbsym_tri Lt, const double *b,
 /* Right-preconditioned GMRES(mr) with ILU0: Lu = unit-lower plan, U = upper
  * plan of the same packed factor.  The preconditioner runs in the dtype
  * the two plans store (FP32 or FP64); SpMV, Arnoldi, Givens and the
- * residual are FP64. */
+ * residual are FP64, all on the device.  1 <= mr <= 1024
+ * (GBSYM_ERR_UNSUPPORTED beyond). */
 int gbsym_gmres(gbsym_csr A, gbsym_tri Lu, gbsym_tri U, const double *b,
                 double *x, int mr, int maxit, double tol,
                 gbsym_krylov_result *res, void *stream);

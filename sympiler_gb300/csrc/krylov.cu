@@ -284,7 +284,9 @@ __device__ __forceinline__ double all_sum(int m, const double *p, double *sh, do
 // any projection into sc[mr+1].  A second round (re-orthogonalisation)
 // runs only when *run_if is set; otherwise block 0 advances the barrier
 // counter by the arrivals the round would have made, and all return.
-__global__ void __launch_bounds__(kRedThreads)
+constexpr int kMgsThreads = 512;
+
+__global__ void __launch_bounds__(kMgsThreads, 2)
 k_mgs_round(long long n, double *V, long long ld, int k, int mr, double *sc, int second,
             const int *run_if, double *part, unsigned *bar, unsigned base, int *err) {
   __shared__ double sh[32];
@@ -301,15 +303,31 @@ k_mgs_round(long long n, double *V, long long ld, int k, int mr, double *sc, int
     const double *vnext = j <= k ? V + (size_t)j * ld : nullptr;
     const bool want_norm = second ? j == k + 1 : (j == 0 || j == k + 1);
     double sd = 0.0, sn = 0.0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-      double vi = v[i];
-      if (vprev) {
-        vi = vi - h * vprev[i];
-        v[i] = vi;
+    // four elements per thread and step, their loads issued together: a
+    // pass streams three vectors, and one element in flight per thread
+    // leaves the memory system idle between round trips
+    const long long step = (long long)gridDim.x * blockDim.x * 4;
+    for (long long i0 = blockIdx.x * (long long)blockDim.x * 4 + threadIdx.x; i0 < n; i0 += step) {
+      double vi[4], vp[4], vn[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const long long i = i0 + (long long)u * blockDim.x;
+        vi[u] = i < n ? v[i] : 0.0;
+        vp[u] = (vprev && i < n) ? vprev[i] : 0.0;
+        vn[u] = (vnext && i < n) ? vnext[i] : 0.0;
       }
-      if (vnext) sd += vi * vnext[i];
-      sn += vi * vi;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const long long i = i0 + (long long)u * blockDim.x;
+        if (i >= n) continue;
+        double x = vi[u];
+        if (vprev) {
+          x = x - h * vp[u];
+          v[i] = x;
+        }
+        if (vnext) sd += x * vn[u];
+        sn += x * x;
+      }
     }
     double *pd = part + (size_t)(j & 1) * 2 * m, *pn = pd + m;
     if (vnext) {
@@ -347,6 +365,7 @@ __global__ void k_scale_by(long long n, const double *__restrict__ alpha, double
 // State (doubles): H[(mr+1) x mr] row-major, c[mr+1], sn[mr+1], g[mr+1],
 // y[mr+1], then the per-step words below.
 enum { GW_SCALE = 0, GW_RHO, GW_CONV, GW_BREAK, GW_COUNT };
+constexpr int kGmresMaxRestart = 1024;
 
 struct GmresState {
   double *H, *c, *sn, *g, *y, *w;  // w: GW_COUNT words
@@ -374,41 +393,59 @@ __global__ void k_gm_column(GmresState st, int k, const double *__restrict__ sc,
 // After the (possibly skipped) second round: its dots added to column k,
 // the scale of v_{k+1}, the earlier rotations applied to column k, the new
 // rotation (mgmres.cpp:927-958, mult_givens 186-251), |g[k+1]| and the
-// convergence and breakdown words.
+// convergence and breakdown words.  The block first loads everything the
+// step reads into shared memory (one round trip instead of one per value
+// on the single thread's dependent chain); thread 0 then computes.
+// Dynamic shared memory: 3(k+2) + 2k doubles.
 __global__ void k_gm_givens(GmresState st, int k, const double *__restrict__ sc, double rho_tol) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  extern __shared__ double gsh[];
   const int mr = st.mr;
-  double *H = st.H;
-  auto Hm = [&](int i, int j) -> double & { return H[i * mr + j]; };
-  if (*st.reorth) {
-    for (int j = 0; j <= k; ++j) Hm(j, k) = add_(Hm(j, k), sc[j]);
-    Hm(k + 1, k) = sqrt(sc[k + 1]);
+  double *col = gsh, *ad = col + (k + 2), *cs = ad + (k + 2), *sns = cs + k, *gg = sns + k;
+  const bool reo = *st.reorth != 0;
+  for (int j = threadIdx.x; j <= k + 1; j += blockDim.x) {
+    col[j] = st.H[j * mr + k];
+    ad[j] = reo ? sc[j] : 0.0;
   }
-  const double hn = Hm(k + 1, k);
-  st.w[GW_SCALE] = hn != 0.0 ? 1.0 / hn : 1.0;
-  for (int j = 0; j < k; ++j) {
-    const double a = Hm(j, k), b = Hm(j + 1, k);
-    Hm(j, k) = sub_(mul_(st.c[j], a), mul_(st.sn[j], b));
-    Hm(j + 1, k) = add_(mul_(st.sn[j], a), mul_(st.c[j], b));
+  for (int j = threadIdx.x; j < k; j += blockDim.x) {
+    cs[j] = st.c[j];
+    sns[j] = st.sn[j];
   }
-  const double mu = sqrt(add_(mul_(Hm(k, k), Hm(k, k)), mul_(Hm(k + 1, k), Hm(k + 1, k))));
-  if (mu == 0.0) {
-    st.w[GW_BREAK] = 1.0;
-    st.w[GW_CONV] = 0.0;
-    return;
+  if (threadIdx.x < 2) gg[threadIdx.x] = st.g[k + threadIdx.x];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (reo) {
+      for (int j = 0; j <= k; ++j) col[j] = add_(col[j], ad[j]);
+      col[k + 1] = sqrt(ad[k + 1]);
+    }
+    const double hn = col[k + 1];
+    st.w[GW_SCALE] = hn != 0.0 ? 1.0 / hn : 1.0;
+    for (int j = 0; j < k; ++j) {
+      const double a = col[j], b = col[j + 1];
+      col[j] = sub_(mul_(cs[j], a), mul_(sns[j], b));
+      col[j + 1] = add_(mul_(sns[j], a), mul_(cs[j], b));
+    }
+    const double mu = sqrt(add_(mul_(col[k], col[k]), mul_(col[k + 1], col[k + 1])));
+    if (mu == 0.0) {
+      st.w[GW_BREAK] = 1.0;
+      st.w[GW_CONV] = 0.0;
+    } else {
+      const double ck = col[k] / mu, sk = -col[k + 1] / mu;
+      st.c[k] = ck;
+      st.sn[k] = sk;
+      col[k] = sub_(mul_(ck, col[k]), mul_(sk, col[k + 1]));
+      col[k + 1] = 0.0;
+      const double g1 = sub_(mul_(ck, gg[0]), mul_(sk, gg[1]));
+      const double g2 = add_(mul_(sk, gg[0]), mul_(ck, gg[1]));
+      st.g[k] = g1;
+      st.g[k + 1] = g2;
+      const double rho = fabs(g2);
+      st.w[GW_RHO] = rho;
+      st.w[GW_CONV] = rho <= rho_tol ? 1.0 : 0.0;
+      st.w[GW_BREAK] = 0.0;
+    }
   }
-  st.c[k] = Hm(k, k) / mu;
-  st.sn[k] = -Hm(k + 1, k) / mu;
-  Hm(k, k) = sub_(mul_(st.c[k], Hm(k, k)), mul_(st.sn[k], Hm(k + 1, k)));
-  Hm(k + 1, k) = 0.0;
-  const double g1 = sub_(mul_(st.c[k], st.g[k]), mul_(st.sn[k], st.g[k + 1]));
-  const double g2 = add_(mul_(st.sn[k], st.g[k]), mul_(st.c[k], st.g[k + 1]));
-  st.g[k] = g1;
-  st.g[k + 1] = g2;
-  const double rho = fabs(g2);
-  st.w[GW_RHO] = rho;
-  st.w[GW_CONV] = rho <= rho_tol ? 1.0 : 0.0;
-  st.w[GW_BREAK] = 0.0;
+  __syncthreads();
+  for (int j = threadIdx.x; j <= k + 1; j += blockDim.x) st.H[j * mr + k] = col[j];
 }
 
 // Restart set-up: g = rho e_1 (mgmres.cpp:878-886); H, c, sn need no
@@ -420,13 +457,23 @@ __global__ void k_gm_start(GmresState st, const double *__restrict__ rr) {
 }
 
 // Back substitution on the rotated H (mgmres.cpp:960-972) into y[0..k].
-__global__ void k_gm_backsub(GmresState st, int k) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  const int mr = st.mr;
-  auto Hm = [&](int i, int j) { return st.H[i * mr + j]; };
-  st.y[k] = st.g[k] / Hm(k, k);
+// With `staged`, the block first copies H's leading (k+1) x (k+1) block and
+// g into shared memory ((k+1)(k+2) doubles of dynamic shared memory), so
+// thread 0's dependent chain reads no global memory.
+__global__ void k_gm_backsub(GmresState st, int k, int staged) {
+  extern __shared__ double bsh[];
+  const int mr = st.mr, w = k + 1;
+  if (staged) {
+    for (int t = threadIdx.x; t < w * w; t += blockDim.x) bsh[t] = st.H[(t / w) * mr + t % w];
+    for (int t = threadIdx.x; t < w; t += blockDim.x) bsh[w * w + t] = st.g[t];
+    __syncthreads();
+  }
+  if (threadIdx.x != 0) return;
+  auto Hm = [&](int i, int j) { return staged ? bsh[i * w + j] : st.H[i * mr + j]; };
+  auto g = [&](int i) { return staged ? bsh[w * w + i] : st.g[i]; };
+  st.y[k] = g(k) / Hm(k, k);
   for (int i = k - 1; i >= 0; --i) {
-    double t = st.g[i];
+    double t = g(i);
     for (int j = i + 1; j < k + 1; ++j) t = sub_(t, mul_(Hm(i, j), st.y[j]));
     st.y[i] = t / Hm(i, i);
   }
@@ -482,6 +529,8 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
            int maxit, double tol, gbsym_krylov_result *res, cudaStream_t s) {
   const long long n = A->n;
   GB_CHECK(mr >= 1 && Lu->n == n && U->n == n && Lu->vdtype == U->vdtype, GBSYM_ERR_SIZE);
+  // the rotation step stages column k in shared memory (5 mr + 6 doubles)
+  GB_CHECK(mr <= kGmresMaxRestart, GBSYM_ERR_UNSUPPORTED);
   const double t0 = now_s();
   const double delta = 1.0e-03;
   DBuf<double> V((size_t)(mr + 1) * n), r(n), w(n), sc(2 * (mr + 2));
@@ -532,7 +581,7 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
   // grid barrier counts arrivals on gbar, whose expected value the host
   // tracks in `base`
   int rs_per_sm = 0;
-  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rs_per_sm, k_mgs_round, kRedThreads, 0));
+  GB_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rs_per_sm, k_mgs_round, kMgsThreads, 0));
   GB_CHECK(rs_per_sm >= 1, GBSYM_ERR_UNSUPPORTED);
   // two blocks per SM: the round's grid barriers cost more with more blocks
   // and its streaming needs enough of them (C3 GMRES, FP32 preconditioner:
@@ -552,7 +601,7 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
     unsigned *barp = gbar.p;
     int *errp = gerr.p;
     void *args[] = {&nn, &Vp, &ld, &kk, &mrr, &scp, &sec, &run_if, &partp, &barp, &base, &errp};
-    GB_CUDA(cudaLaunchCooperativeKernel((const void *)k_mgs_round, dim3(rblocks), dim3(kRedThreads), args, 0, s));
+    GB_CUDA(cudaLaunchCooperativeKernel((const void *)k_mgs_round, dim3(rblocks), dim3(kMgsThreads), args, 0, s));
     check_launch();
     base += (unsigned)(k + 2) * rblocks;
   };
@@ -592,7 +641,7 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
       k_gm_column<<<1, 32, 0, s>>>(st, k, sc.p, delta);
       check_launch();
       mgs_round(k, true);
-      k_gm_givens<<<1, 32, 0, s>>>(st, k, sc.p, rho_tol);
+      k_gm_givens<<<1, 32, (size_t)(5 * k + 6) * sizeof(double), s>>>(st, k, sc.p, rho_tol);
       check_launch();
       k_scale_by<<<eb, 256, 0, s>>>(n, st.w + GW_SCALE, Vj(k + 1));
       check_launch();
@@ -614,7 +663,11 @@ void gmres(gbsym_csr_s *A, gbsym_tri_s *Lu, gbsym_tri_s *U, const double *b, dou
     const int kk = k_stop >= 0 ? k_stop : k_last;
     itr_used += kk + 1;
     if (k_stop >= 0) converged = true;
-    k_gm_backsub<<<1, 32, 0, s>>>(st, kk);
+    {
+      const size_t bs = (size_t)(kk + 1) * (kk + 2) * sizeof(double);
+      const bool staged = bs <= 48 * 1024;
+      k_gm_backsub<<<1, 256, staged ? bs : 0, s>>>(st, kk, staged ? 1 : 0);
+    }
     check_launch();
     k_combine<<<eb, 256, 0, s>>>(n, kk + 1, V.p, n, st.y, r.p);
     check_launch();
