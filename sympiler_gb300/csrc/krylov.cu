@@ -284,9 +284,9 @@ __device__ __forceinline__ double all_sum(int m, const double *p, double *sh, do
 // any projection into sc[mr+1].  A second round (re-orthogonalisation)
 // runs only when *run_if is set; otherwise block 0 advances the barrier
 // counter by the arrivals the round would have made, and all return.
-constexpr int kMgsThreads = 512;
+constexpr int kMgsThreads = 256;
 
-__global__ void __launch_bounds__(kMgsThreads, 2)
+__global__ void __launch_bounds__(kMgsThreads)
 k_mgs_round(long long n, double *V, long long ld, int k, int mr, double *sc, int second,
             const int *run_if, double *part, unsigned *bar, unsigned base, int *err) {
   __shared__ double sh[32];
@@ -303,31 +303,15 @@ k_mgs_round(long long n, double *V, long long ld, int k, int mr, double *sc, int
     const double *vnext = j <= k ? V + (size_t)j * ld : nullptr;
     const bool want_norm = second ? j == k + 1 : (j == 0 || j == k + 1);
     double sd = 0.0, sn = 0.0;
-    // four elements per thread and step, their loads issued together: a
-    // pass streams three vectors, and one element in flight per thread
-    // leaves the memory system idle between round trips
-    const long long step = (long long)gridDim.x * blockDim.x * 4;
-    for (long long i0 = blockIdx.x * (long long)blockDim.x * 4 + threadIdx.x; i0 < n; i0 += step) {
-      double vi[4], vp[4], vn[4];
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const long long i = i0 + (long long)u * blockDim.x;
-        vi[u] = i < n ? v[i] : 0.0;
-        vp[u] = (vprev && i < n) ? vprev[i] : 0.0;
-        vn[u] = (vnext && i < n) ? vnext[i] : 0.0;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x) {
+      double vi = v[i];
+      if (vprev) {
+        vi = vi - h * vprev[i];
+        v[i] = vi;
       }
-#pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const long long i = i0 + (long long)u * blockDim.x;
-        if (i >= n) continue;
-        double x = vi[u];
-        if (vprev) {
-          x = x - h * vp[u];
-          v[i] = x;
-        }
-        if (vnext) sd += x * vn[u];
-        sn += x * x;
-      }
+      if (vnext) sd += vi * vnext[i];
+      sn += vi * vi;
     }
     double *pd = part + (size_t)(j & 1) * 2 * m, *pn = pd + m;
     if (vnext) {
