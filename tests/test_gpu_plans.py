@@ -435,6 +435,20 @@ def test_batch_uneven_systems(gpu, orc):
         a, z = bp.offsets[q], bp.offsets[q + 1]
         ref = _oracle_mrhs(orc, L, B[a:z])
         assert np.array_equal(got[a:z], ref), q
+    # the batch solve captured in a CUDA graph and replayed on new inputs
+    side = torch.cuda.Stream()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g, stream=side):
+        bp.solve(x)
+    for replay in range(2):
+        B2 = rng.standard_normal((N, k))
+        x.copy_(torch.from_numpy(B2))
+        g.replay()
+        torch.cuda.synchronize()
+        got = x.cpu().numpy()
+        for q in (0, len(Ls) // 2, len(Ls) - 1):
+            a, z = bp.offsets[q], bp.offsets[q + 1]
+            assert np.array_equal(got[a:z], _oracle_mrhs(orc, Ls[q], B2[a:z])), (replay, q)
 
 
 def test_lower_csc_plan_matches_column_push_oracle(gpu, orc):
