@@ -561,6 +561,81 @@ def fp32_mrhs(L, dev, stream, flush, k=64):
             "executors": {"k%d" % k: ek, "k1": e1}}
 
 
+def fp64_mrhs(L, dev, stream, flush, k=64):
+    """FP64, k right-hand sides, out of place, exact arithmetic, on a lower
+    CSR factor: time, GB/s, HBM fraction and the FP64 roofline."""
+    import torch
+    from sympiler_gb300._lib import EXEC_NAMES
+    from sympiler_gb300.plans import TriPlan
+    P = TriPlan(L.n, *L.astuple())
+    ek = EXEC_NAMES.get(P.autotune(k=k))
+    B = torch.from_numpy(np.random.default_rng(65).standard_normal((L.n, k))).to(dev)
+    X = torch.empty_like(B)
+    t = _time(lambda: P.solve_into(B, X), 7, stream, flush)
+    P.check()
+    info = P.info()
+    peak, src = hbm_peak()
+    byt = algorithmic_bytes(L.nnz, L.n, k)
+    ops = fp64_ops_exact(int(info.nnz_off), L.n, k)
+    return {"n": L.n, "levels": info.levels, "rhs": k, "ms": t * 1e3, "gbs": byt / t / 1e9,
+            "frac": byt / t / 1e9 / peak, "peak_source": src, "fp64_frac": ops / t / 1e9 / FP64_PEAK_GOPS,
+            "fp64_floor_ms": ops / FP64_PEAK_GOPS / 1e6, "executor": ek}
+
+
+def bench_c1(dev, stream, flush):
+    """C1, the reference's CPU-runnable case: L = lower triangle of the 2D
+    5-point Laplacian on a 100 x 100 grid (n = 10,000, 199 levels), one
+    right-hand side, FP64; and SpMV with the full Laplacian.  The GPU solve
+    is timed cold (L2 flushed) and warm (back to back); beside it the
+    oracle's serial sptrsv_csr and spmv_csr on one host core (CPU leg
+    only).  A problem this small is latency-bound on the GPU: 199 dependent
+    levels cost more than a serial CPU solve that fits in L1/L2."""
+    import torch
+    from sympiler_gb300 import matgen as mg
+    from sympiler_gb300._lib import EXEC_NAMES
+    from sympiler_gb300.plans import CsrPlan, TriPlan
+    A = mg.lap2d(100)
+    L = mg.tril(A)
+    P = TriPlan(L.n, *L.astuple())
+    e1 = EXEC_NAMES.get(P.autotune(k=1))
+    b = torch.from_numpy(np.random.default_rng(1).uniform(-1, 1, L.n)).to(dev)
+    x = torch.empty_like(b)
+    t_cold = _time(lambda: P.solve_into(b, x), 15, stream, flush)
+    t_warm = _time(lambda: P.solve_into(b, x), 15, stream, None)
+    P.check()
+    Ap = CsrPlan(A.n, *A.astuple())
+    y = torch.empty_like(b)
+    t_spmv = _time(lambda: Ap.spmv(b, y), 15, stream, flush)
+    trsv_b = algorithmic_bytes(L.nnz, L.n, 1)
+    spmv_b = 12 * A.nnz + 4 * (A.n + 1) + 16 * A.n
+    out = {"n": L.n, "levels": P.info().levels, "executor": e1,
+           "sptrsv_us_cold": t_cold * 1e6, "sptrsv_us_warm": t_warm * 1e6,
+           "sptrsv_solves_per_s": 1.0 / t_warm, "sptrsv_gbs_cold": trsv_b / t_cold / 1e9,
+           "spmv_us_cold": t_spmv * 1e6, "spmv_gbs_cold": spmv_b / t_spmv / 1e9}
+    try:
+        import oracle
+        o = oracle.orc()
+        bh = b.cpu().numpy()
+        ts = []
+        for _ in range(21):
+            xh = bh.copy()
+            t0 = time.perf_counter()
+            o.sptrsv_csr(L.n, *L.astuple(), xh)
+            ts.append(time.perf_counter() - t0)
+        yh = np.zeros(A.n)
+        tsp = []
+        for _ in range(21):
+            t0 = time.perf_counter()
+            o.spmv_csr(A.n, *A.astuple(), bh, yh)
+            tsp.append(time.perf_counter() - t0)
+        out["cpu_port"] = {"sptrsv_us": statistics.median(ts) * 1e6, "spmv_us": statistics.median(tsp) * 1e6,
+                           "cores": 1, "cpu": host_cpu(),
+                           "bit_identical": bool(np.array_equal(xh, x.cpu().numpy()))}
+    except Exception as ex:  # the baseline must not hide the GPU numbers
+        out["cpu_port"] = {"error": str(ex)}
+    return out
+
+
 def bench_adjoint(dev, stream, flush, g=1024, k=32):
     """Forward X = L^{-1} B and the reverse pass (L^T solve + value gradient)
     on the IC0 factor of the 1024^2 anisotropic variable-coefficient Poisson
@@ -601,7 +676,8 @@ def bench_adjoint(dev, stream, flush, g=1024, k=32):
     info = Lf.info()
     byt = algorithmic_bytes(Lcsr.nnz, U.n, k)
     fp32 = fp32_mrhs(Lcsr, dev, stream, flush, 64)
-    return {"fp32_64rhs": fp32, "n": U.n, "nnz_L": Lcsr.nnz, "levels": info.levels, "rhs": k,
+    fp64 = fp64_mrhs(Lcsr, dev, stream, flush, 64)
+    return {"fp32_64rhs": fp32, "fp64_64rhs": fp64, "n": U.n, "nnz_L": Lcsr.nnz, "levels": info.levels, "rhs": k,
             "forward_ms": tf * 1e3, "forward_gbs": byt / tf / 1e9, "backward_ms": tb * 1e3,
             "executors": {"forward": ef, "transposed": et}}
 
@@ -1162,6 +1238,8 @@ def main():
         extras["batch_c4"] = bench_batch(dev, stream, flush, extras["sptrsv_64rhs_fp32_c2"]["hop_us"])
         extras["adjoint_c5"] = bench_adjoint(dev, stream, flush)
         extras["sptrsv_64rhs_fp32_c5"] = extras["adjoint_c5"].pop("fp32_64rhs")
+        extras["sptrsv_64rhs_fp64_c5"] = extras["adjoint_c5"].pop("fp64_64rhs")
+        extras["c1_lap2d_100"] = bench_c1(dev, stream, flush)
         extras["spmv"] = bench_spmv(dev, stream, flush)
         extras["supernodal_c2_nd"] = bench_supernodal(dev, stream, flush)
         result["extras"] = extras
