@@ -396,7 +396,8 @@ def bench_batch(dev, stream, flush, hop_us=None, k=8):
         byt = algorithmic_bytes(nnz, N, k, vb, vb)
         res[dt] = {"ms": t * 1e3, "batch_solves_per_s": 1.0 / t, "gbs": byt / t / 1e9,
                    "frac": byt / t / 1e9 / peak, "peak_gbs": peak, "peak_source": src,
-                   "levels": info.levels, "executor": chosen, "hbm_floor_ms": byt / peak / 1e6}
+                   "levels": info.levels, "executor": chosen, "tuning": bp.tuning(k),
+                   "hbm_floor_ms": byt / peak / 1e6}
         if hop_us:
             res[dt]["floor_ms"] = max(byt / peak / 1e6, info.levels * hop_us / 1e3)
             res[dt]["floor_note"] = "max(HBM floor, levels x %.2f us one-RHS FP32 hop on the C2 factor)" % hop_us
@@ -818,7 +819,8 @@ def run_c4(args):
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
                 "higher_is_better": True, "scaling": "strong", "vs_baseline": None, "dtype": dt,
                 "data": "synthetic", "config": dict(c4_config(dt, k, len(idx), world), rows_rank0=N,
-                                                    levels_rank0=info.levels, executor=chosen),
+                                                    levels_rank0=info.levels, executor=chosen,
+                                                    tuning=bp.tuning(k)),
                 "roofline": {"bound": "hbm", "achieved": byt / t_step / 1e9, "peak": peak, "unit": "GB/s",
                              "frac": byt / t_step / 1e9 / peak, "peak_source": peak_src,
                              "traffic": load_traffic("c4_batch_%s_8rhs" % dt),

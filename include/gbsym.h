@@ -443,6 +443,12 @@ int gbsym_tri_set_arith(gbsym_tri t, int arith);
  * chosen GBSYM_EXEC_* is returned in *chosen when non-NULL.  Synchronises
  * the stream. */
 int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, int *chosen);
+/* The executor settings solves with k right-hand sides use (after
+ * gbsym_tri_autotune, the tuned ones): tuning[0] the GBSYM_EXEC_*,
+ * tuning[1] the sync-free sweep's blocks per SM (0: its default by k),
+ * tuning[2] its lane layout (1: the alternative, k > 1 only).  No
+ * counterpart in the reference. */
+int gbsym_tri_get_tuning(gbsym_tri t, int k, int *tuning);
 /* Waits for `stream` and returns the first error a device-side check of
  * this plan recorded since the last call (e.g. GBSYM_ERR_TIMEOUT from a
  * bounded wait), clearing it; GBSYM_OK when none. */
@@ -572,6 +578,8 @@ int gbsym_batch_autotune(gbsym_batch b, int k, int dtype, void *stream, int *cho
 int gbsym_batch_check(gbsym_batch b, void *stream);
 /* Size, levels and storage of the pooled triangle. */
 int gbsym_batch_get_info(gbsym_batch b, gbsym_tri_info *info);
+/* gbsym_tri_get_tuning of the batch's pool. */
+int gbsym_batch_get_tuning(gbsym_batch b, int k, int *tuning);
 
 /* ---- forward solve that allocates nothing ------------------------------ */
 /* No counterpart in the reference.  For callers that cannot allocate device

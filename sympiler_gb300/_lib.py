@@ -121,6 +121,8 @@ SIGNATURES = {
     "gbsym_batch_autotune": (_int, [_vp, _int, _int, _vp, _pi]),
     "gbsym_batch_check": (_int, [_vp, _vp]),
     "gbsym_batch_get_info": (_int, [_vp, C.POINTER(TriInfo)]),
+    "gbsym_batch_get_tuning": (_int, [_vp, _int, _pi]),
+    "gbsym_tri_get_tuning": (_int, [_vp, _int, _pi]),
     "gbsym_sptrsv_csr_noalloc": (_int, [_int, _vp, _vp, _vp, _vp, _vp]),
 }
 

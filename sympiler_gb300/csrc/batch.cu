@@ -127,6 +127,11 @@ extern "C" int gbsym_batch_get_info(gbsym_batch b, gbsym_tri_info *info) {
   return gbsym_tri_get_info(b->pool.get(), info);
 }
 
+extern "C" int gbsym_batch_get_tuning(gbsym_batch b, int k, int *tuning) {
+  if (!b) return GBSYM_ERR_NULL_ARG;
+  return gbsym_tri_get_tuning(b->pool.get(), k, tuning);
+}
+
 extern "C" int gbsym_batch_row_offsets(gbsym_batch b, long long *offsets) {
   if (!b || !offsets) return GBSYM_ERR_NULL_ARG;
   for (int q = 0; q <= b->nsys; ++q) offsets[q] = b->off[q];

@@ -241,6 +241,15 @@ extern "C" int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, i
   });
 }
 
+extern "C" int gbsym_tri_get_tuning(gbsym_tri t, int k, int *tuning) {
+  if (!t || !tuning) return GBSYM_ERR_NULL_ARG;
+  if (k < 1) return GBSYM_ERR_SIZE;
+  tuning[0] = effective_exec(t, k, false);
+  tuning[1] = t->sf_blocks_per_sm > 0 ? t->sf_blocks_per_sm : t->sf_bps_tuned[k > 1 ? 1 : 0];
+  tuning[2] = k > 1 ? t->sf_alt_lanes : 0;
+  return GBSYM_OK;
+}
+
 extern "C" int gbsym_tri_set_arith(gbsym_tri t, int arith) {
   if (!t) return GBSYM_ERR_NULL_ARG;
   if (arith != GBSYM_ARITH_EXACT && arith != GBSYM_ARITH_FUSED) return GBSYM_ERR_UNSUPPORTED;

@@ -107,6 +107,12 @@ class TriPlan:
         check(lib().gbsym_tri_get_info(self._h, C.byref(inf)), "gbsym_tri_get_info")
         return inf
 
+    def tuning(self, k=1) -> dict:
+        """Executor settings used for k right-hand sides (gbsym_tri_get_tuning)."""
+        v = (C.c_int * 3)()
+        check(lib().gbsym_tri_get_tuning(self._h, int(k), v), "gbsym_tri_get_tuning")
+        return {"exec": v[0], "blocks_per_sm": v[1], "alt_lanes": v[2]}
+
     def schedule(self):
         inf = self.info()
         lp = np.zeros(inf.levels + 1, dtype=np.int32)
@@ -368,6 +374,12 @@ class BatchPlan:
         inf = TriInfo()
         check(lib().gbsym_batch_get_info(self._h, C.byref(inf)), "gbsym_batch_get_info")
         return inf
+
+    def tuning(self, k=1) -> dict:
+        """Executor settings used for k right-hand sides (gbsym_batch_get_tuning)."""
+        v = (C.c_int * 3)()
+        check(lib().gbsym_batch_get_tuning(self._h, int(k), v), "gbsym_batch_get_tuning")
+        return {"exec": v[0], "blocks_per_sm": v[1], "alt_lanes": v[2]}
 
     def autotune(self, k=1, dtype=None, stream=None) -> int:
         """Time the executors on the batch for k right-hand sides; returns the chosen one."""
