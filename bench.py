@@ -68,18 +68,49 @@ def algorithmic_bytes(nnz_l, n, k, vbytes=8, sbytes=8):
     return (vbytes + 4) * nnz_l + 4 * (n + 1) + 2 * sbytes * k * n
 
 
-# FP64 throughput of this GB300 (dependent-free DFMA stream, all SMs): 597 G
-# operations/s (502 G for separate multiplies and adds), measured by a
-# microbenchmark during development.  On this part the FP64 pipe, not HBM,
-# bounds an FP64 triangular solve; the exact kernels issue every rounded
-# operation as an FMA.
-FP64_PEAK_GOPS = 597.0
+_FP64_RATES = None
+
+
+def fp64_rates():
+    """(update, fma) FP64 throughput of this GPU in G op/s, measured once per
+    process by the library's probe (gbsym_fp64_rates): the exact update's
+    rounded product and rounded difference, and general three-operand FMAs.
+    GB300 runs the first form about 1.7x as fast as the second."""
+    global _FP64_RATES
+    if _FP64_RATES is None:
+        import ctypes as C
+        from sympiler_gb300._lib import check, lib
+        u, f = C.c_double(), C.c_double()
+        check(lib().gbsym_fp64_rates(C.byref(u), C.byref(f), None), "gbsym_fp64_rates")
+        _FP64_RATES = (u.value, f.value)
+    return _FP64_RATES
 
 
 def fp64_ops_exact(nnz_off, n, k):
     """FP64 operations of one exact solve: a multiply and a subtract per
     stored off-diagonal, three for the correctly rounded division."""
     return k * (2 * nnz_off + 3 * n)
+
+
+def fp64_floor_s(nnz_off, n, k):
+    """FP64-pipe time floor of one exact solve: per right-hand side,
+    2 nnz_off + n update-class operations (each entry's product and
+    difference, the division's first product) at the update rate, and 2 n
+    general FMAs (the division's remainder and correction) at the FMA rate."""
+    u, f = fp64_rates()
+    return k * (2 * nnz_off + n) / (u * 1e9) + k * 2 * n / (f * 1e9)
+
+
+def fp64_roofline(nnz_off, n, k, t):
+    """FP64 roofline of one exact solve taking t seconds."""
+    ops = fp64_ops_exact(nnz_off, n, k)
+    floor = fp64_floor_s(nnz_off, n, k)
+    u, f = fp64_rates()
+    return {"bound": "fp64 pipe", "achieved": ops / t / 1e9, "peak": ops / floor / 1e9,
+            "unit": "G FP64 op/s", "frac": floor / t, "ops_per_solve": ops, "floor_ms": floor * 1e3,
+            "rates_gops": {"update": u, "fma": f},
+            "peak_source": "measured live (gbsym_fp64_rates); peak = the op mix's rate: "
+                           "updates at the update rate, the division's two general FMAs at the FMA rate"}
 
 
 def config(grid, k):
@@ -430,7 +461,7 @@ def bench_spmv(dev, stream, flush):
         byt = 12 * A.nnz + 4 * (A.n + 1) + 16 * A.n
         out[name] = {"n": A.n, "nnz": int(A.nnz), "us": t * 1e6, "gbs": byt / t / 1e9,
                      "hbm_frac": byt / t / 1e9 / peak,
-                     "fp64_gops": 2 * A.nnz / t / 1e9, "fp64_frac": 2 * A.nnz / t / 1e9 / FP64_PEAK_GOPS}
+                     "fp64_gops": 2 * A.nnz / t / 1e9, "fp64_frac": 2 * A.nnz / t / 1e9 / fp64_rates()[0]}
         # spmv_csr_parallel on all host cores (CPU baseline leg only)
         try:
             import oracle
@@ -491,7 +522,7 @@ def bench_supernodal(dev, stream, flush, grid=64):
             t = _time(run, 5 if k == 1 else 3, stream, flush)
             P.check()
             key = "%s_k%d" % ("transposed" if tr else "forward", k)
-            out[key] = {"ms": t * 1e3, "fp64_gops": ops / t / 1e9, "fp64_frac": ops / t / 1e9 / FP64_PEAK_GOPS,
+            out[key] = {"ms": t * 1e3, "fp64_gops": ops / t / 1e9, "fp64_frac": ops / t / 1e9 / fp64_rates()[0],
                         "gbs": byt / t / 1e9}
     # end to end with host buffers, factor resident: H2D, solve, D2H
     hx = torch.from_numpy(rng.standard_normal(S.n)).pin_memory()
@@ -579,8 +610,9 @@ def fp64_mrhs(L, dev, stream, flush, k=64):
     byt = algorithmic_bytes(L.nnz, L.n, k)
     ops = fp64_ops_exact(int(info.nnz_off), L.n, k)
     return {"n": L.n, "levels": info.levels, "rhs": k, "ms": t * 1e3, "gbs": byt / t / 1e9,
-            "frac": byt / t / 1e9 / peak, "peak_source": src, "fp64_frac": ops / t / 1e9 / FP64_PEAK_GOPS,
-            "fp64_floor_ms": ops / FP64_PEAK_GOPS / 1e6, "executor": ek}
+            "frac": byt / t / 1e9 / peak, "peak_source": src,
+            "fp64_frac": fp64_floor_s(int(info.nnz_off), L.n, k) / t,
+            "fp64_floor_ms": fp64_floor_s(int(info.nnz_off), L.n, k) * 1e3, "executor": ek}
 
 
 def bench_c1(dev, stream, flush):
@@ -1020,11 +1052,7 @@ def main():
                                   if tuned["k%d" % k] == "levelset" else
                                   "one solve = the sentinel fill of X + one %s kernel launch" % tuned["k%d" % k])
                                  + "; duration from CUDA events on the launch stream"},
-            "roofline_fp64": {"bound": "fp64 pipe", "achieved": fp64_ops_exact(int(info.nnz_off), n, k) / t_step / 1e9,
-                              "peak": FP64_PEAK_GOPS, "unit": "G FP64 op/s",
-                              "frac": fp64_ops_exact(int(info.nnz_off), n, k) / t_step / 1e9 / FP64_PEAK_GOPS,
-                              "ops_per_solve": fp64_ops_exact(int(info.nnz_off), n, k),
-                              "peak_source": "measured (DFMA throughput microbenchmark, this pool)"},
+            "roofline_fp64": fp64_roofline(int(info.nnz_off), n, k, t_step),
             "e2e": {"value": byt / e2e_step / 1e9, "unit": UNIT, "h2d_bytes_per_step": n * k * 8,
                     "d2h_bytes_per_step": n * k * 8, "ms_per_step": e2e_step * 1e3,
                     "api": "gbsym_tri_solve_host (pinned host x, row-major, wall clock per call)",

@@ -458,6 +458,13 @@ int gbsym_tri_check(gbsym_tri t, void *stream);
  * (at most 10 s).  Returns GBSYM_ERR_TIMEOUT when the wait gave up and
  * reported it, which is the expected outcome; the context stays usable. */
 int gbsym_selftest_bounded_wait(long long limit_ns, void *stream);
+/* No counterpart in the reference: a measurement aid for roofline figures.
+ * Measures this GPU's FP64 throughput, in G operations/s, for the two forms
+ * the exact solves issue: the update acc = RN(acc - RN(v*x)) (a rounded
+ * product and a rounded difference: *update_gops) and general fused
+ * multiply-adds with three variable operands (the division's remainder and
+ * correction steps: *fma_gops).  Two short kernels; synchronises `stream`. */
+int gbsym_fp64_rates(double *update_gops, double *fma_gops, void *stream);
 /* Copy the schedule into host buffers of levels+1 and n ints. */
 int gbsym_tri_get_schedule(gbsym_tri t, int *level_ptr, int *level_set);
 

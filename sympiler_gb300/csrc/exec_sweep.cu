@@ -235,6 +235,67 @@ template void run_persist<float>(gbsym_tri_s *, float *, int, cudaStream_t);
 
 }  // namespace gbsym
 
+namespace gbsym {
+
+// FP64 throughput probe: every thread runs two independent chains of
+// MODE 0: the exact update acc = RN(acc - RN(v*x)) as the sweeps issue it,
+// MODE 1: general fused multiply-adds with three variable operands (the
+// form of the division's remainder and correction steps).
+// The operands pass through an empty asm each iteration so that no part of
+// an update can be hoisted out of the loop.
+template <int MODE>
+__global__ void __launch_bounds__(256) k_fp64_rate(int iters, double *out) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  double v[2], x[2], a[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    v[c] = 1e-4 * (1 + ((t * 7 + c * 3) & 15));
+    x[c] = 1.0 + 0.01 * ((t + c) & 31);
+    a[c] = 10.0 + c + 0.001 * (t & 63);
+  }
+  for (int it = 0; it < iters; ++it) {
+#pragma unroll
+    for (int c = 0; c < 2; ++c) {
+      asm volatile("" : "+d"(x[c]), "+d"(v[c]));
+      if (MODE == 0) a[c] = msub<kArithExact>(a[c], v[c], x[c]);
+      else a[c] = __fma_rn(__fma_rn(a[c], v[c], x[c]), x[c], v[c]);
+    }
+  }
+  out[t] = a[0] + a[1];
+}
+
+template <int MODE>
+static double fp64_rate(double *out, cudaStream_t s) {
+  const int grid = 4 * num_sms(), iters = 4096;
+  cudaEvent_t e0, e1;
+  GB_CUDA(cudaEventCreate(&e0));
+  GB_CUDA(cudaEventCreate(&e1));
+  k_fp64_rate<MODE><<<grid, 256, 0, s>>>(iters / 8, out);  // warm-up
+  check_launch();
+  GB_CUDA(cudaEventRecord(e0, s));
+  k_fp64_rate<MODE><<<grid, 256, 0, s>>>(iters, out);
+  check_launch();
+  GB_CUDA(cudaEventRecord(e1, s));
+  GB_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return 2.0 * 2.0 * grid * 256.0 * iters / (ms * 1e-3) / 1e9;  // two ops per update, two chains
+}
+
+}  // namespace gbsym
+
+extern "C" int gbsym_fp64_rates(double *update_gops, double *fma_gops, void *stream) {
+  if (!update_gops || !fma_gops) return GBSYM_ERR_NULL_ARG;
+  return gbsym::guarded([&] {
+    cudaStream_t s = (cudaStream_t)stream;
+    gbsym::DBuf<double> out((size_t)4 * gbsym::num_sms() * 256);
+    *update_gops = gbsym::fp64_rate<0>(out.p, s);
+    *fma_gops = gbsym::fp64_rate<1>(out.p, s);
+  });
+}
+
 extern "C" int gbsym_selftest_bounded_wait(long long limit_ns, void *stream) {
   if (limit_ns <= 0 || limit_ns > 10000000000ll) return GBSYM_ERR_SIZE;
   int code = GBSYM_OK;
