@@ -167,6 +167,7 @@ k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ 
       unsigned got = 0;
       const unsigned need = (1u << ns) - 1u;
       int jo = A.K;          // next overflow dependency
+      bool slab_done = false;  // the slab's updates are in acc
       T acc[VEC];
       if (!done) vload<T, VEC, false>(rhs + (size_t)rs.orig * k + r, acc);
       long long t0 = clock_now();
@@ -195,18 +196,35 @@ k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ 
             got |= 1u << q;
             moved = true;
           }
-        // overflow dependencies, OVB per round: their column indices and
-        // values are loaded together, then taken in order while ready
+        // overflow dependencies, OVB per round, once the slab is complete:
+        // the slab's updates are applied first (storage order), then each
+        // overflow value is applied as soon as it and the ones before it
+        // are ready -- no second round trip to load them again
         if constexpr (OVB > 0) {
-          if (jo < rs.len) {
-            T v[OVB][VEC];
+          if (got == need && jo < rs.len) {
+            if (!slab_done) {
+#pragma unroll
+              for (int q = 0; q < KS; ++q)
+                if (q < ns) {
+#pragma unroll
+                  for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], rs.v[q], xv[q][w]);
+                }
+              slab_done = true;
+            }
+            T v[OVB][VEC], a[OVB];
 #pragma unroll
             for (int b = 0; b < OVB; ++b)
-              if (jo + b < rs.len) ld_rlx<T, VEC>(y + (size_t)A.oci[rs.ovb + jo + b - A.K] * k + r, v[b]);
+              if (jo + b < rs.len) {
+                const int e = rs.ovb + jo + b - A.K;
+                ld_rlx<T, VEC>(y + (size_t)A.oci[e] * k + r, v[b]);
+                a[b] = A.ov[e];
+              }
             bool run = true;
 #pragma unroll
             for (int b = 0; b < OVB; ++b)
               if (run && jo < rs.len && all_ready<T, VEC>(v[b])) {
+#pragma unroll
+                for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], a[b], v[b][w]);
                 ++jo;
                 moved = true;
               } else {
@@ -246,30 +264,14 @@ k_syncfree(TriView<T> A, T *x, T *y, const T *b, int k, const int *__restrict__ 
         }
       }
       if (active && r < k) {
+        // the slab's updates, unless the overflow polling applied them
+        if (!slab_done) {
 #pragma unroll
-        for (int q = 0; q < KS; ++q)
-          if (q < ns) {
+          for (int q = 0; q < KS; ++q)
+            if (q < ns) {
 #pragma unroll
-            for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], rs.v[q], xv[q][w]);
-          }
-        // overflow entries in storage order, OVB loads in flight
-        if constexpr (OVB > 0) {
-          for (int t = A.K; t < rs.len; t += OVB) {
-            T v[OVB][VEC], a[OVB];
-#pragma unroll
-            for (int b = 0; b < OVB; ++b)
-              if (t + b < rs.len) {
-                const int e = rs.ovb + t + b - A.K;
-                ld_rlx<T, VEC>(y + (size_t)A.oci[e] * k + r, v[b]);
-                a[b] = A.ov[e];
-              }
-#pragma unroll
-            for (int b = 0; b < OVB; ++b)
-              if (t + b < rs.len) {
-#pragma unroll
-                for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], a[b], v[b][w]);
-              }
-          }
+              for (int w = 0; w < VEC; ++w) acc[w] = msub<AR>(acc[w], rs.v[q], xv[q][w]);
+            }
         }
         T out[VEC];
 #pragma unroll
