@@ -303,15 +303,37 @@ k_mgs_round(long long n, double *V, long long ld, int k, int mr, double *sc, int
     const double *vnext = j <= k ? V + (size_t)j * ld : nullptr;
     const bool want_norm = second ? j == k + 1 : (j == 0 || j == k + 1);
     double sd = 0.0, sn = 0.0;
-    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
-         i += (long long)gridDim.x * blockDim.x) {
-      double vi = v[i];
-      if (vprev) {
-        vi = vi - h * vprev[i];
-        v[i] = vi;
+    // the thread's elements i, i + S, i + 2S, ... in that order (so the
+    // sums are those of a plain grid-stride loop), four at a time with all
+    // their loads issued before the first store: the stores to v would
+    // otherwise keep every load of the next element behind them, one
+    // memory round trip per element
+    constexpr int U = 4;
+    const long long S = (long long)gridDim.x * blockDim.x;
+    for (long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x; i0 < n; i0 += U * S) {
+      double a[U], p[U], q[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long i = i0 + u * S;
+        if (i < n) {
+          a[u] = v[i];
+          if (vprev) p[u] = vprev[i];
+          if (vnext) q[u] = vnext[i];
+        }
       }
-      if (vnext) sd += vi * vnext[i];
-      sn += vi * vi;
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const long long i = i0 + u * S;
+        if (i < n) {
+          double vi = a[u];
+          if (vprev) {
+            vi = vi - h * p[u];
+            v[i] = vi;
+          }
+          if (vnext) sd += vi * q[u];
+          sn += vi * vi;
+        }
+      }
     }
     double *pd = part + (size_t)(j & 1) * 2 * m, *pn = pd + m;
     if (vnext) {
