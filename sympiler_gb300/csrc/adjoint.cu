@@ -106,6 +106,7 @@ using namespace gbsym;
 
 extern "C" int gbsym_tri_adjoint(gbsym_tri Lt, int n, const int *Lp, const int *Li, const double *X,
                                  double *g, int k, double *grad, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_tri_adjoint");
   if (!Lt || (n && (!Lp || !Li || !X || !g || !grad))) return GBSYM_ERR_NULL_ARG;
   return guarded([&] {
     tri_adjoint(Lt, n, Lp, Li, X, g, k, grad, (cudaStream_t)stream);

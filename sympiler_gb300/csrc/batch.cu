@@ -89,12 +89,14 @@ static int batch_create(gbsym_batch *out, int nsys, const int *n, const int *con
 extern "C" int gbsym_batch_create(gbsym_batch *out, int nsys, const int *n, const int *const *Lp,
                                   const int *const *Li, const double *const *Lx, int value_dtype,
                                   void *stream) {
+  gbsym::PhaseRange phase_("gbsym_batch_create");
   return batch_create(out, nsys, n, Lp, Li, Lx, GBSYM_LOWER_DIAG_LAST, value_dtype, stream);
 }
 
 extern "C" int gbsym_batch_create_kind(gbsym_batch *out, int nsys, const int *n, const int *const *Lp,
                                        const int *const *Li, const double *const *Lx, int kind,
                                        int value_dtype, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_batch_create_kind");
   return batch_create(out, nsys, n, Lp, Li, Lx, kind, value_dtype, stream);
 }
 
@@ -104,6 +106,7 @@ extern "C" int gbsym_batch_destroy(gbsym_batch b) {
 }
 
 extern "C" int gbsym_batch_solve(gbsym_batch b, void *x, int k, int dtype, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_batch_solve");
   if (!b || (!x && b->off.back() && k)) return GBSYM_ERR_NULL_ARG;
   if (k < 1) return GBSYM_ERR_SIZE;
   return guarded([&] {
@@ -113,6 +116,7 @@ extern "C" int gbsym_batch_solve(gbsym_batch b, void *x, int k, int dtype, void 
 }
 
 extern "C" int gbsym_batch_autotune(gbsym_batch b, int k, int dtype, void *stream, int *chosen) {
+  gbsym::PhaseRange phase_("gbsym_batch_autotune");
   if (!b) return GBSYM_ERR_NULL_ARG;
   return gbsym_tri_autotune(b->pool.get(), k, dtype, stream, chosen);
 }

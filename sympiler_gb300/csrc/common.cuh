@@ -11,6 +11,7 @@
 #include <vector>
 
 #include "gbsym.h"
+#include "nvtx3/nvToolsExt.h"
 
 namespace gbsym {
 
@@ -50,6 +51,17 @@ int guarded(F &&f) {
     return GBSYM_ERR_SIZE;
   }
 }
+
+// A named NVTX range around one call of a library phase (plan build,
+// factorisation, solve, Krylov iteration, batch), so that Nsight timelines
+// show where a caller's time goes.  Header-only NVTX: without a tool
+// attached a push or pop is a check of a function pointer.
+struct PhaseRange {
+  explicit PhaseRange(const char *name) { nvtxRangePushA(name); }
+  ~PhaseRange() { nvtxRangePop(); }
+  PhaseRange(const PhaseRange &) = delete;
+  PhaseRange &operator=(const PhaseRange &) = delete;
+};
 
 // Every kernel launch made by the library goes through this counter.
 extern std::atomic<unsigned long long> g_launches;

@@ -223,6 +223,7 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
 using namespace gbsym;
 
 extern "C" int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, int *chosen) {
+  gbsym::PhaseRange phase_("gbsym_tri_autotune");
   if (!t) return GBSYM_ERR_NULL_ARG;
   if (k < 1) return GBSYM_ERR_SIZE;
   return guarded([&] {

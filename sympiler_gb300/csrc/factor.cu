@@ -265,6 +265,7 @@ using namespace gbsym;
 
 extern "C" int gbsym_ilu0_device(int n, const int *Ap, const int *Ai, const double *Ax,
                                  const int *A_diag, double *l, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_ilu0_device");
   if (n > 0 && (!Ap || !Ai || !Ax || !A_diag || !l)) return GBSYM_ERR_NULL_ARG;
   return guarded([&] {
     ilu0_device(n, Ap, Ai, Ax, A_diag, l, (cudaStream_t)stream);
@@ -273,6 +274,7 @@ extern "C" int gbsym_ilu0_device(int n, const int *Ap, const int *Ai, const doub
 
 extern "C" int gbsym_ic0_device(int n, double *val, const int *rowPtr, const int *rowIdx,
                                 void *stream) {
+  gbsym::PhaseRange phase_("gbsym_ic0_device");
   if (n > 0 && (!val || !rowPtr || !rowIdx)) return GBSYM_ERR_NULL_ARG;
   return guarded([&] {
     ic0_device(n, val, rowPtr, rowIdx, (cudaStream_t)stream);

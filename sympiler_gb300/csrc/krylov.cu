@@ -706,6 +706,7 @@ using namespace gbsym;
 
 extern "C" int gbsym_pcg(gbsym_csr A, gbsym_tri L, gbsym_tri Lt, const double *b, double *x,
                          double tol, int maxit, gbsym_krylov_result *res, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_pcg");
   if (!A || !L || !Lt || (A->n && (!b || !x))) return GBSYM_ERR_NULL_ARG;
   return guarded([&] {
     pcg(A, L, Lt, b, x, tol, maxit, res, (cudaStream_t)stream);
@@ -714,6 +715,7 @@ extern "C" int gbsym_pcg(gbsym_csr A, gbsym_tri L, gbsym_tri Lt, const double *b
 
 extern "C" int gbsym_gmres(gbsym_csr A, gbsym_tri Lu, gbsym_tri U, const double *b, double *x,
                            int mr, int maxit, double tol, gbsym_krylov_result *res, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_gmres");
   if (!A || !Lu || !U || (A->n && (!b || !x))) return GBSYM_ERR_NULL_ARG;
   return guarded([&] {
     gmres(A, Lu, U, b, x, mr, maxit, tol, res, (cudaStream_t)stream);

@@ -171,6 +171,7 @@ extern "C" int gbsym_csr_destroy(gbsym_csr a) {
 }
 
 extern "C" int gbsym_csr_spmv(gbsym_csr a, const void *x, void *y, int dtype, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_csr_spmv");
   if (!a || (a->n && (!x || !y))) return GBSYM_ERR_NULL_ARG;
   return guarded([&] {
     csr_spmv(a, x, y, dtype, (cudaStream_t)stream);

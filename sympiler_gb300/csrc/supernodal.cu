@@ -965,6 +965,7 @@ extern "C" {
 
 int gbsym_sn_create(gbsym_sn *out, int n, const size_t *Lp, const int *Li, const double *Lx, const size_t *Li_ptr,
                     const int *sup2col, int supNo, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_sn_create");
   if (!out) return GBSYM_ERR_NULL_ARG;
   *out = nullptr;
   return guarded([&] { *out = sn_build(n, Lp, Li, Lx, Li_ptr, sup2col, supNo, (cudaStream_t)stream); });
@@ -983,6 +984,7 @@ int gbsym_sn_levels(gbsym_sn t, int *forward_levels, int *transposed_levels) {
 }
 
 int gbsym_sn_solve(gbsym_sn t, double *x, int k, int transposed, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_sn_solve");
   if (!t || (!x && t->n && k)) return GBSYM_ERR_NULL_ARG;
   if (k < 0) return GBSYM_ERR_SIZE;
   return guarded([&] { sn_solve(t, x, k, transposed != 0, (cudaStream_t)stream); });

@@ -647,6 +647,7 @@ extern "C" int gbsym_tri_create(gbsym_tri *out, int n, const int *p, const int *
                                 const int *diags, int kind, int value_dtype, int on_device,
                                 const int *level_ptr, const int *level_set, int levels,
                                 void *stream) {
+  gbsym::PhaseRange phase_("gbsym_tri_create");
   if (!out || (n > 0 && (!p || !i || !x))) return GBSYM_ERR_NULL_ARG;
   *out = nullptr;
   return guarded([&] {
@@ -742,6 +743,7 @@ extern "C" int gbsym_tri_get_schedule(gbsym_tri t, int *level_ptr, int *level_se
 }
 
 extern "C" int gbsym_tri_solve(gbsym_tri t, void *x, int k, int layout, int dtype, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_tri_solve");
   if (!t || (!x && t->n && k)) return GBSYM_ERR_NULL_ARG;
   if (k < 0) return GBSYM_ERR_SIZE;
   return guarded([&] {
@@ -761,6 +763,7 @@ extern "C" int gbsym_tri_solve(gbsym_tri t, void *x, int k, int layout, int dtyp
 }
 
 extern "C" int gbsym_tri_solve_into(gbsym_tri t, const void *b, void *x, int k, int dtype, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_tri_solve_into");
   if (!t || (t->n && k > 0 && (!x || !b))) return GBSYM_ERR_NULL_ARG;
   if (k < 0) return GBSYM_ERR_SIZE;
   return guarded([&] {
@@ -771,6 +774,7 @@ extern "C" int gbsym_tri_solve_into(gbsym_tri t, const void *b, void *x, int k, 
 }
 
 extern "C" int gbsym_tri_solve_b(gbsym_tri t, const double *b, double *x, void *stream) {
+  gbsym::PhaseRange phase_("gbsym_tri_solve_b");
   if (!t || (t->n && (!x || !b))) return GBSYM_ERR_NULL_ARG;
   return guarded([&] {
     cudaStream_t s = (cudaStream_t)stream;
@@ -807,6 +811,7 @@ extern "C" int gbsym_host_solve_in_place(const void *x) {
 }
 
 extern "C" int gbsym_tri_solve_host(gbsym_tri t, double *x, int k, int layout) {
+  gbsym::PhaseRange phase_("gbsym_tri_solve_host");
   if (!t || (!x && t->n && k)) return GBSYM_ERR_NULL_ARG;
   if (k < 0) return GBSYM_ERR_SIZE;
   return guarded([&] {
