@@ -821,30 +821,44 @@ def run_c4(args):
     Lt0 = sp.csr_matrix((x0, i0, p0), shape=(n0, n0))
     xs = X[:n0, 0].double().cpu().numpy()
     resid = float(np.abs(Lt0.T @ xs - B[:n0, 0].double().cpu().numpy()).max())
-    # end to end: pinned host right-hand sides in, solution out, every step
+    # end to end through the C ABI on pinned host buffers
+    # (gbsym_batch_solve_host).  With 8 right-hand sides a row's values are
+    # 32 or 64 bytes, below the 256 bytes from which the library solves a
+    # page-locked buffer in place over the CPU-GPU link, so it stages
+    # H2D + solve + D2H (in place measured 7.9 / 15.9 ms against 6.4 /
+    # 13.1 ms staged).
+    from sympiler_gb300.plans import host_solve_in_place
     Hb = torch.empty((N, k), dtype=tdt).pin_memory()
     Hb.copy_(B.cpu())
     Hx = torch.empty_like(Hb).pin_memory()
 
-    def e2e_once():
-        X.copy_(Hb, non_blocking=True)
-        bp.solve(X)
-        Hx.copy_(X, non_blocking=True)
-        torch.cuda.synchronize()
-    for _ in range(2):
-        e2e_once()
-    te = []
-    for _ in range(max(3, args.steps // 2)):
-        flush.fill_(rank + 1)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        e2e_once()
-        te.append(time.perf_counter() - t0)
-    e2e_t = statistics.median(te)
+    def e2e_median(direct):
+        if direct:
+            os.environ.pop("GBSYM_HOST_DIRECT", None)
+        else:
+            os.environ["GBSYM_HOST_DIRECT"] = "0"
+        for _ in range(2):
+            Hx.copy_(Hb)
+            bp.solve_host(Hx)
+        ts = []
+        for _ in range(max(3, args.steps // 2)):
+            Hx.copy_(Hb)
+            flush.fill_(rank + 1)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            bp.solve_host(Hx)
+            ts.append(time.perf_counter() - t0)
+        os.environ.pop("GBSYM_HOST_DIRECT", None)
+        return statistics.median(ts)
+
+    e2e_staged = e2e_median(False)
+    e2e_t = e2e_median(True)
+    in_place = host_solve_in_place(Hx.data_ptr()) and k * vb >= 256
+    e2e_exact = bool(torch.equal(Hx, X.cpu()))
     if world > 1:
-        tt = torch.tensor([e2e_t], device=dev)
+        tt = torch.tensor([e2e_t, e2e_staged], device=dev)
         torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        e2e_t = float(tt.item())
+        e2e_t, e2e_staged = float(tt[0].item()), float(tt[1].item())
     peak, peak_src = hbm_peak()
     if rank == 0:
         line = {"metric": METRIC, "value": byt_all / t_step / 1e9, "unit": UNIT, "n_gpus": world,
@@ -859,7 +873,13 @@ def run_c4(args):
                              "algorithmic_bytes_per_solve": byt},
                 "e2e": {"value": byt_all / e2e_t / 1e9, "unit": UNIT, "h2d_bytes_per_step": N * k * vb,
                         "d2h_bytes_per_step": N * k * vb, "ms_per_step": e2e_t * 1e3,
-                        "api": "BatchPlan.solve (gbsym_batch_solve) between pinned-host copies"},
+                        "api": "BatchPlan.solve_host (gbsym_batch_solve_host, pinned host x, row-major, "
+                               "wall clock per call)",
+                        "path": ("in place over the CPU-GPU link (sync-free sweep reads b and writes x in "
+                                 "the host buffer)") if in_place else "staged: H2D + solve + D2H",
+                        "bit_identical_to_device_solve": e2e_exact,
+                        "staged_ms_per_step": e2e_staged * 1e3,
+                        "staged_value": byt_all / e2e_staged / 1e9},
                 "gpu_launches": int(launches), "clocks": clocks,
                 "check": {"max_abs_residual_system0_col0": resid}}
         print(json.dumps(line), flush=True)

@@ -577,6 +577,13 @@ int gbsym_batch_destroy(gbsym_batch b);
  * or FP32).  offsets (host, nsys+1) receives the row offset of each system
  * when non-NULL. */
 int gbsym_batch_solve(gbsym_batch b, void *x, int k, int dtype, void *stream);
+/* As gbsym_batch_solve on HOST memory (row-major, the batch's dtype).  When
+ * x is page-locked, the GPU shares the host's page tables (Grace +
+ * NVLink-C2C) and a row's k values take at least 256 bytes, the sweep reads
+ * each right-hand side and writes each result across the link once, in
+ * place; otherwise the solve is staged through a device copy (bulk copies
+ * serve short rows faster).  Synchronises. */
+int gbsym_batch_solve_host(gbsym_batch b, void *x, int k, int dtype);
 int gbsym_batch_row_offsets(gbsym_batch b, long long *offsets);
 /* Executor choice for k right-hand sides, timed on the batch itself (as
  * gbsym_tri_autotune on the pooled triangle). */

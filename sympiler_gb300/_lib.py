@@ -70,6 +70,7 @@ SIGNATURES = {
     "gbsym_tri_check": (_int, [_vp, _vp]),
     "gbsym_selftest_bounded_wait": (_int, [_ll, _vp]),
     "gbsym_fp64_rates": (_int, [_vp, _vp, _vp]),
+    "gbsym_batch_solve_host": (_int, [_vp, _vp, _int, _int]),
     "gbsym_tri_set_arith": (_int, [_vp, _int]),
     "gbsym_tri_autotune": (_int, [_vp, _int, _int, _vp, _pi]),
     "gbsym_tri_get_schedule": (_int, [_vp, _vp, _vp]),

@@ -115,6 +115,13 @@ extern "C" int gbsym_batch_solve(gbsym_batch b, void *x, int k, int dtype, void 
   });
 }
 
+extern "C" int gbsym_batch_solve_host(gbsym_batch b, void *x, int k, int dtype) {
+  gbsym::PhaseRange phase_("gbsym_batch_solve_host");
+  if (!b || (!x && b->off.back() && k)) return GBSYM_ERR_NULL_ARG;
+  if (k < 1) return GBSYM_ERR_SIZE;
+  return guarded([&] { tri_solve_host_rowmajor(b->pool.get(), x, k, dtype); });
+}
+
 extern "C" int gbsym_batch_autotune(gbsym_batch b, int k, int dtype, void *stream, int *chosen) {
   gbsym::PhaseRange phase_("gbsym_batch_autotune");
   if (!b) return GBSYM_ERR_NULL_ARG;

@@ -136,6 +136,9 @@ namespace gbsym {
 // selects the "redundant" row formula (k == 1, FP64 only).
 void tri_solve_rowmajor(gbsym_tri_s *t, void *x, const void *b, int k, int dtype,
                         cudaStream_t s);
+// Row-major host memory (FP64 or FP32 as the plan), in place over the
+// CPU-GPU link where the buffer allows it, else staged; synchronises.
+void tri_solve_host_rowmajor(gbsym_tri_s *t, void *x, int k, int dtype);
 // Out of place on device memory, row-major n x k: x = L^-1 b, b unchanged
 // (b and x must not overlap).
 void tri_solve_into(gbsym_tri_s *t, const void *b, void *x, int k, int dtype, cudaStream_t s);

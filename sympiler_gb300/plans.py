@@ -399,6 +399,16 @@ class BatchPlan:
               "gbsym_batch_solve")
         return x
 
+    def solve_host(self, x):
+        """Solve in place on a host tensor (row-major, the batch's dtype): over
+        the CPU-GPU link when x is page-locked on a coherent system, else
+        staged.  Synchronises."""
+        assert x.device.type == "cpu" and x.is_contiguous()
+        k = 1 if x.dim() == 1 else x.shape[1]
+        check(lib().gbsym_batch_solve_host(self._h, C.c_void_p(x.data_ptr()), int(k), _dtype_code(x.dtype)),
+              "gbsym_batch_solve_host")
+        return x
+
     def close(self):
         if getattr(self, "_h", None):
             lib().gbsym_batch_destroy(self._h)

@@ -1,5 +1,7 @@
 """Device-resident plans at the workload sizes: multi-RHS, FP32, executors,
 layouts, end-to-end host solves -- against the oracle."""
+import ctypes as C
+
 import numpy as np
 import pytest
 import torch
@@ -452,6 +454,51 @@ def test_batch_uneven_systems(gpu, orc):
         for q in (0, len(Ls) // 2, len(Ls) - 1):
             a, z = bp.offsets[q], bp.offsets[q + 1]
             assert np.array_equal(got[a:z], _oracle_mrhs(orc, Ls[q], B2[a:z])), (replay, q)
+
+
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+@pytest.mark.parametrize("k", [8, 64])
+def test_batch_host_buffers(gpu, orc, dtype, k):
+    """gbsym_batch_solve_host: page-locked host buffers (in place over the
+    CPU-GPU link where the system allows it and rows hold 256 bytes or
+    more, else staged) and pageable ones (staged) give the device solve's
+    bits; FP64 against the oracle as well."""
+    from sympiler_gb300._lib import lib
+    from sympiler_gb300.plans import BatchPlan
+    rng = np.random.default_rng(41)
+    systems, Ls = [], []
+    for q in range(6):
+        if q % 3 == 2:
+            A = mg.random_spd(int(rng.integers(200, 1500)), 8, rng)
+        else:
+            A = mg.lap2d(int(rng.integers(20, 50)), int(rng.integers(20, 50)))
+            A = mg.from_scipy(A.scipy() + 0.5 * __import__("scipy").sparse.eye(A.n))
+        U = mg.triu(A)
+        f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+        assert ok
+        L = mg.transpose(mg.CSR(U.n, U.p, U.i, f))
+        Ls.append(L)
+        systems.append((L.n, *L.astuple()))
+    bp = BatchPlan(systems, dtype=dtype)
+    tdt = torch.float64 if dtype == "f64" else torch.float32
+    N = int(bp.offsets[-1])
+    B = torch.from_numpy(rng.standard_normal((N, k))).to(tdt)
+    xd = B.clone().cuda()
+    bp.solve(xd)
+    torch.cuda.synchronize()
+    want = xd.cpu()
+    pinned = B.clone().pin_memory()
+    bp.solve_host(pinned)
+    assert torch.equal(pinned, want)
+    pageable = B.clone()
+    bp.solve_host(pageable)
+    assert torch.equal(pageable, want)
+    assert lib().gbsym_host_solve_in_place(C.c_void_p(pageable.data_ptr())) == 0
+    if dtype == "f64":
+        got = pinned.numpy()
+        for q, L in enumerate(Ls):
+            a, z = bp.offsets[q], bp.offsets[q + 1]
+            assert np.array_equal(got[a:z], _oracle_mrhs(orc, L, B.numpy()[a:z])), q
 
 
 def test_lower_csc_plan_matches_column_push_oracle(gpu, orc):
