@@ -446,8 +446,10 @@ int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, int *chosen)
 /* The executor settings solves with k right-hand sides use (after
  * gbsym_tri_autotune, the tuned ones): tuning[0] the GBSYM_EXEC_*,
  * tuning[1] the sync-free sweep's blocks per SM (0: its default by k),
- * tuning[2] its lane layout (1: the alternative, k > 1 only).  No
- * counterpart in the reference. */
+ * tuning[2] for k > 1 its lane layout (1: the alternative), for k = 1
+ * whether it looks through one level (1: the spare lanes of each row
+ * recompute its dependencies, so rows wait two levels back; plans whose
+ * rows fit a three-entry slab).  No counterpart in the reference. */
 int gbsym_tri_get_tuning(gbsym_tri t, int k, int *tuning);
 /* Waits for `stream` and returns the first error a device-side check of
  * this plan recorded since the last call (e.g. GBSYM_ERR_TIMEOUT from a

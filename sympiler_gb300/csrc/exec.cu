@@ -17,7 +17,7 @@
 #include <tuple>
 #include <vector>
 
-#include "exec_common.cuh"
+#include "exec_syncfree.cuh"
 
 namespace gbsym {
 
@@ -67,6 +67,7 @@ void choose_exec(gbsym_tri_s *t) {
   if (const char *cb = std::getenv("GBSYM_CLUSTER_BLOCKS")) t->cluster_blocks = std::atoi(cb);
   if (const char *sb = std::getenv("GBSYM_SF_BLOCKS_PER_SM")) t->sf_blocks_per_sm = std::atoi(sb);
   if (const char *al = std::getenv("GBSYM_SF_ALT_LANES")) t->sf_alt_lanes = std::atoi(al) == 1;
+  if (const char *lt = std::getenv("GBSYM_SF_LOOKTHROUGH")) t->sf_lookthrough = std::atoi(lt) != 0;
   t->sf_deal = num_sms();
   if (const char *sd = std::getenv("GBSYM_SF_DEAL")) t->sf_deal = std::atoi(sd);
 }
@@ -149,6 +150,10 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
                                             {GBSYM_EXEC_SYNCFREE, 3}, {GBSYM_EXEC_CLUSTER, 0}};
   if (k > 1)
     for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | 8});
+  // one right-hand side on a plan that allows it: the look-through sweep
+  // (bit 4) beside the plain one
+  if (k == 1 && sf_lookthrough_ok(t))
+    for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | 16});
   if (k == 1 && t->max_level_rows <= 4096) cands.push_back({GBSYM_EXEC_ONEBLOCK, 0});
   if (k == 1) {
     std::vector<int> sizes;
@@ -171,13 +176,14 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   float best_ms = 0;
   const int saved_rows = t->part_rows_pref;
   const int kk = k > 1 ? 1 : 0;
-  const int saved_bps = t->sf_bps_tuned[kk], saved_alt = t->sf_alt_lanes;
+  const int saved_bps = t->sf_bps_tuned[kk], saved_alt = t->sf_alt_lanes, saved_lt = t->sf_lookthrough;
   for (const auto &cand : cands) {
     const int e = cand.first;
     if (e == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = cand.second;
     if (e == GBSYM_EXEC_SYNCFREE) {
       t->sf_bps_tuned[kk] = cand.second & 7;
-      if (k > 1) t->sf_alt_lanes = cand.second >> 3;
+      if (k > 1) t->sf_alt_lanes = (cand.second >> 3) & 1;
+      else t->sf_lookthrough = (cand.second >> 4) & 1;
     }
     std::vector<float> ms;
     for (int rep = 0; rep < 4; ++rep) {
@@ -206,11 +212,13 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   t->part_rows_pref = saved_rows;
   t->sf_bps_tuned[kk] = saved_bps;
   t->sf_alt_lanes = saved_alt;
+  t->sf_lookthrough = saved_lt;
   if (best < 0) throw Err{GBSYM_ERR_TIMEOUT};
   if (best == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = best_rows;
   if (best == GBSYM_EXEC_SYNCFREE) {
     t->sf_bps_tuned[kk] = best_rows & 7;
-    if (k > 1) t->sf_alt_lanes = best_rows >> 3;
+    if (k > 1) t->sf_alt_lanes = (best_rows >> 3) & 1;
+    else t->sf_lookthrough = (best_rows >> 4) & 1;
   }
   if (k == 1) t->exec = best; else t->exec_mrhs = best;
   std::lock_guard<std::mutex> lk(g_tuned_mu);
@@ -247,7 +255,7 @@ extern "C" int gbsym_tri_get_tuning(gbsym_tri t, int k, int *tuning) {
   if (k < 1) return GBSYM_ERR_SIZE;
   tuning[0] = effective_exec(t, k, false);
   tuning[1] = t->sf_blocks_per_sm > 0 ? t->sf_blocks_per_sm : t->sf_bps_tuned[k > 1 ? 1 : 0];
-  tuning[2] = k > 1 ? t->sf_alt_lanes : 0;
+  tuning[2] = k > 1 ? t->sf_alt_lanes : (t->sf_lookthrough && sf_lookthrough_ok(t) ? 1 : 0);
   return GBSYM_OK;
 }
 

@@ -1,0 +1,176 @@
+// exec_sf_lt.cu -- the sync-free sweep for one right-hand side with
+// look-through: every row waits on values two levels back instead of one.
+//
+// With one right-hand side a row takes four lanes of which one computes;
+// here the other three each recompute one of the row's dependencies from
+// that dependency's own row data and right-hand side.  Row i needs x_j for
+// its dependencies j; lane q+1 rebuilds x_j = (b_j - sum L_jm x_m) / L_jj
+// with the same operation sequence the owner of row j uses (storage order,
+// separately rounded products and differences, the same division), so the
+// value is bit-identical to the one j's owner publishes.  A row therefore
+// waits only for its dependencies' dependencies, and each publish -> poll
+// hop of the sweep (the L2 round trip that bounds one-right-hand-side
+// solves) now advances the wavefront by two levels, at the cost of a second
+// dependent FP64 chain per row and of loads the idle lanes would not make.
+//
+// Every row is still computed and published by its owner, so rows whose
+// dependencies look through to it see its value as before.  The solve is
+// in place: the right-hand sides are first gathered into a packed-order
+// copy (other rows read b_j there, since x_j is overwritten when row j
+// finishes), the published values go to the plan's packed scratch.  Used
+// for plans whose rows all fit a slab of at most three entries (the three
+// spare lanes cover every dependency) and no overflow entries.
+//
+// Deadlock freedom is the plain sweep's argument: a unit waits only on
+// values of rows at least two levels earlier, which belong to earlier
+// units, every warp walks its units in order and the launch is cooperative.
+#include <algorithm>
+
+#include "exec_syncfree_kernel.cuh"
+
+namespace gbsym {
+
+// b copied into packed order and the scratch set to the sentinel, in one pass
+template <class T>
+__global__ void k_lt_prep(int n, const int *__restrict__ perm, const T *__restrict__ x, T *__restrict__ bp,
+                          T *__restrict__ y) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    bp[r] = x[perm[r]];
+    if constexpr (sizeof(T) == 8) reinterpret_cast<unsigned long long *>(y)[r] = ~0ull;
+    else reinterpret_cast<unsigned *>(y)[r] = ~0u;
+  }
+}
+
+template <class T, int AR, int KS>
+__global__ void __launch_bounds__(kSfBlock, 3)
+k_syncfree_lt(TriView<T> A, T *x, T *y, const T *__restrict__ bp, const int *__restrict__ unit_row,
+              const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & 3;    // 0: the row itself; q + 1: its dependency q
+  const int sub = lane >> 2;  // row of the unit (eight rows per warp unit)
+  const int warp = deal_warp(nsm);
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int u = warp; u < nunits; u += nwarps) {
+    const bool active = sub < unit_cnt[u];
+    const int row = unit_row[u] + sub;
+    const int rlen = active ? min(A.len[row], A.K) : 0;
+    // lane 0 holds row `row`; lane q + 1 holds dependency q of it
+    const bool work = active && (gl == 0 || gl - 1 < rlen);
+    const int me = !work ? 0 : (gl == 0 ? row : A.sci[(size_t)(gl - 1) * A.npad + row]);
+    RowStatic<T, KS> rs;
+    if (work) load_row(A, me, rs);
+    T acc = work ? bp[me] : T(0);
+    // dependency lanes poll the values their row reads: two rounds of loads
+    // in flight, as in the plain sweep's one-value lanes
+    const bool dep = work && gl > 0;
+    const int ns = dep ? min(rs.len, A.K) : 0;
+    const unsigned need = (1u << ns) - 1u;
+    unsigned got = 0;
+    T xv[KS], va[KS], vb[KS];
+    bool done = !dep || ns == 0;
+    auto issue = [&](T (&buf)[KS]) {
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < ns && !((got >> q) & 1u)) {
+          T v[1];
+          ld_rlx<T, 1>(y + rs.c[q], v);
+          buf[q] = v[0];
+        }
+    };
+    auto absorb = [&](T (&buf)[KS]) {
+      bool moved = false;
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < ns && !((got >> q) & 1u) && !is_sentinel(buf[q])) {
+          xv[q] = buf[q];
+          got |= 1u << q;
+          moved = true;
+        }
+      if (got == need) done = true;
+      return moved;
+    };
+    if (!done) issue(va);
+    long long t0 = clock_now();
+    int rounds = 0;
+    bool odd = false;
+    while (__any_sync(FULL, !done)) {
+      bool moved = false;
+      if (!done) {
+        if (!odd) {
+          issue(vb);
+          moved = absorb(va);
+        } else {
+          issue(va);
+          moved = absorb(vb);
+        }
+        if (moved) t0 = clock_now();
+      }
+      odd = !odd;
+      if (!__any_sync(FULL, moved)) __nanosleep(32);
+      if ((++rounds & 63) == 0) {
+        if (!done && clock_now() - t0 > kWaitLimitCycles) {
+          atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
+          done = true;
+        }
+        const int e = lane == 0 ? ld_relaxed(err) : 0;
+        if (__shfl_sync(FULL, e, 0) != 0) return;
+      }
+    }
+    // dependency lanes: x_j exactly as row j's owner computes it
+    T xj = T(0);
+    if (dep) {
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < ns) acc = msub<AR>(acc, rs.v[q], xv[q]);
+      xj = row_finish(A, rs, acc);
+    }
+    const int base = lane & ~3;
+    T d[3];
+    d[0] = __shfl_sync(FULL, xj, base + 1);
+    d[1] = __shfl_sync(FULL, xj, base + 2);
+    d[2] = __shfl_sync(FULL, xj, base + 3);
+    if (work && gl == 0) {
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < rlen) acc = msub<AR>(acc, rs.v[q], d[q]);
+      const T out = row_finish(A, rs, acc);
+      x[rs.orig] = out;
+      T o[1] = {not_sentinel(out)};
+      st_rlx<T, 1>(y + row, o);
+    }
+  }
+}
+
+template <class T, int AR, int KS>
+static void lt_launch(gbsym_tri_s *t, T *x, T *y, const T *bp, cudaStream_t s) {
+  const TriView<T> A = view_packed_of<T>(t);
+  const Units U = sf_units(t, 8);
+  launch_coop(t, 1, k_syncfree_lt<T, AR, KS>, s, A, x, y, bp, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+}
+
+template <class T>
+void run_syncfree_lt(gbsym_tri_s *t, T *x, cudaStream_t s) {
+  GB_CHECK(t->K <= 3 && t->nov == 0, GBSYM_ERR_UNSUPPORTED);
+  const size_t bytes = (size_t)t->n * sizeof(T);
+  t->sfy.reserve(bytes);
+  t->sfb.reserve(bytes);
+  T *y = reinterpret_cast<T *>(t->sfy.p);
+  T *bp = reinterpret_cast<T *>(t->sfb.p);
+  const int grid = std::max(1, std::min(div_up(t->n, 256), num_sms() * 8));
+  k_lt_prep<T><<<grid, 256, 0, s>>>(t->n, t->perm.p, x, bp, y);
+  check_launch();
+  const bool fused = t->arith == kArithFused;
+  if (t->K <= 2) {
+    if (fused) lt_launch<T, kArithFused, 2>(t, x, y, bp, s);
+    else lt_launch<T, kArithExact, 2>(t, x, y, bp, s);
+  } else {
+    if (fused) lt_launch<T, kArithFused, 3>(t, x, y, bp, s);
+    else lt_launch<T, kArithExact, 3>(t, x, y, bp, s);
+  }
+}
+
+template void run_syncfree_lt<double>(gbsym_tri_s *, double *, cudaStream_t);
+template void run_syncfree_lt<float>(gbsym_tri_s *, float *, cudaStream_t);
+
+}  // namespace gbsym

@@ -267,20 +267,24 @@ __global__ void __launch_bounds__(256) k_fp64_rate(int iters, double *out) {
 template <int MODE>
 static double fp64_rate(double *out, cudaStream_t s) {
   const int grid = 4 * num_sms(), iters = 4096;
-  cudaEvent_t e0, e1;
-  GB_CUDA(cudaEventCreate(&e0));
-  GB_CUDA(cudaEventCreate(&e1));
+  struct Events {
+    cudaEvent_t e[2] = {nullptr, nullptr};
+    ~Events() {
+      for (auto v : e)
+        if (v) cudaEventDestroy(v);
+    }
+  } ev;
+  GB_CUDA(cudaEventCreate(&ev.e[0]));
+  GB_CUDA(cudaEventCreate(&ev.e[1]));
   k_fp64_rate<MODE><<<grid, 256, 0, s>>>(iters / 8, out);  // warm-up
   check_launch();
-  GB_CUDA(cudaEventRecord(e0, s));
+  GB_CUDA(cudaEventRecord(ev.e[0], s));
   k_fp64_rate<MODE><<<grid, 256, 0, s>>>(iters, out);
   check_launch();
-  GB_CUDA(cudaEventRecord(e1, s));
-  GB_CUDA(cudaEventSynchronize(e1));
+  GB_CUDA(cudaEventRecord(ev.e[1], s));
+  GB_CUDA(cudaEventSynchronize(ev.e[1]));
   float ms = 0.f;
-  GB_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
+  GB_CUDA(cudaEventElapsedTime(&ms, ev.e[0], ev.e[1]));
   return 2.0 * 2.0 * grid * 256.0 * iters / (ms * 1e-3) / 1e9;  // two ops per update, two chains
 }
 

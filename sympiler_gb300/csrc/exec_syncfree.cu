@@ -51,6 +51,10 @@ void fill_sentinel(void *y, size_t bytes, cudaStream_t s) {
 
 template <class T>
 void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s, const T *b) {
+  if (k == 1 && !b && t->sf_lookthrough && sf_lookthrough_ok(t)) {
+    run_syncfree_lt<T>(t, x, s);
+    return;
+  }
   const size_t bytes = (size_t)t->n * k * sizeof(T);
   T *y = x;
   if (!b) {

@@ -26,4 +26,10 @@ Units sf_units(gbsym_tri_s *t, int rpw);
 template <class T, int KS, bool OV>
 void sf_run_ks(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s);
 
+// One right-hand side, in place, with look-through (exec_sf_lt.cu): plans
+// whose rows all fit a slab of at most three entries.
+inline bool sf_lookthrough_ok(const gbsym_tri_s *t) { return t->K <= 3 && t->nov == 0; }
+template <class T>
+void run_syncfree_lt(gbsym_tri_s *t, T *x, cudaStream_t s);
+
 }  // namespace gbsym

@@ -85,6 +85,7 @@ struct gbsym_tri_s {
   gbsym::DBuf<int> err;              // device error word(s): code, where
   gbsym::DBuf<unsigned> bar;         // grid-barrier arrival counter
   gbsym::DBuf<char> sfy;             // sync-free published values (sentinel-filled)
+  gbsym::DBuf<char> sfb;             // look-through sweep: right-hand side in packed order
   struct SfUnits {
     int rpw = 0, n = 0;
     gbsym::DBuf<int> row, cnt;       // level-aligned warp units
@@ -95,6 +96,9 @@ struct gbsym_tri_s {
   int sf_alt_lanes = 0;              // k > 1, 1: the other lane layout (FP64: two values per
                                      // lane; FP32: two), the autotuner's choice
   int sf_deal = 0;                   // sync-free unit dealing: SM count to spread over (0: plain order)
+  int sf_lookthrough = 1;            // k = 1: spare lanes recompute each row's dependencies, so
+                                     // rows wait two levels back (exec_sf_lt.cu); plans whose
+                                     // rows fit a three-entry slab, 0: the plain sweep
   struct PartPlan {
     int R = 0, nparts = 0, ngroups = 0;  // rows per partition (0: not built)
     gbsym::DBuf<int> part_group, group_ptr, rows;

@@ -108,10 +108,12 @@ class TriPlan:
         return inf
 
     def tuning(self, k=1) -> dict:
-        """Executor settings used for k right-hand sides (gbsym_tri_get_tuning)."""
+        """Executor settings used for k right-hand sides (gbsym_tri_get_tuning):
+        the executor, the sync-free blocks per SM, and for k > 1 the lane
+        layout (alt_lanes), for k = 1 the look-through sweep (lookthrough)."""
         v = (C.c_int * 3)()
         check(lib().gbsym_tri_get_tuning(self._h, int(k), v), "gbsym_tri_get_tuning")
-        return {"exec": v[0], "blocks_per_sm": v[1], "alt_lanes": v[2]}
+        return {"exec": v[0], "blocks_per_sm": v[1], ("alt_lanes" if k > 1 else "lookthrough"): v[2]}
 
     def schedule(self):
         inf = self.info()
@@ -379,7 +381,7 @@ class BatchPlan:
         """Executor settings used for k right-hand sides (gbsym_batch_get_tuning)."""
         v = (C.c_int * 3)()
         check(lib().gbsym_batch_get_tuning(self._h, int(k), v), "gbsym_batch_get_tuning")
-        return {"exec": v[0], "blocks_per_sm": v[1], "alt_lanes": v[2]}
+        return {"exec": v[0], "blocks_per_sm": v[1], ("alt_lanes" if k > 1 else "lookthrough"): v[2]}
 
     def autotune(self, k=1, dtype=None, stream=None) -> int:
         """Time the executors on the batch for k right-hand sides; returns the chosen one."""

@@ -1,0 +1,101 @@
+"""The one-right-hand-side look-through sweep (spare lanes recompute each
+row's dependencies so that rows wait two levels back) against the plain
+sync-free sweep and the oracle, bit for bit, for every row form it serves:
+lower CSR with the diagonal last, unit lower and upper ILU factors, the
+transposed (upper) solve, FP64 and FP32, exact and fused arithmetic.  Plans
+whose rows do not fit a three-entry slab fall back to the plain sweep."""
+import numpy as np
+import pytest
+import torch
+
+from sympiler_gb300 import matgen as mg
+
+pytestmark = pytest.mark.gpu
+
+
+def _plan(monkeypatch, lookthrough, *args, **kw):
+    from sympiler_gb300._lib import EXEC_SYNCFREE
+    from sympiler_gb300.plans import TriPlan
+    monkeypatch.setenv("GBSYM_SF_LOOKTHROUGH", "1" if lookthrough else "0")
+    P = TriPlan(*args, **kw)
+    monkeypatch.delenv("GBSYM_SF_LOOKTHROUGH")
+    P.set_exec(EXEC_SYNCFREE)
+    return P
+
+
+def _solve(P, b, dtype=torch.float64):
+    x = torch.from_numpy(b.copy()).to(dtype).cuda()
+    P.solve(x)
+    P.check()
+    return x.cpu().numpy()
+
+
+@pytest.mark.parametrize("grid", [(60, 50), (24, 20, 16)])
+def test_lower_fp64_fp32_exact_and_fused(gpu, orc, monkeypatch, grid):
+    from sympiler_gb300._lib import ARITH_FUSED
+    A = mg.lap2d(*grid) if len(grid) == 2 else mg.lap3d(grid[0], 1e-2)
+    U = mg.triu(A)
+    f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+    assert ok
+    L = mg.transpose(mg.CSR(U.n, U.p, U.i, f))
+    b = np.random.default_rng(5).standard_normal(L.n)
+    ref = b.copy()
+    orc.sptrsv_csr(L.n, *L.astuple(), ref)
+    on = _plan(monkeypatch, True, L.n, *L.astuple())
+    off = _plan(monkeypatch, False, L.n, *L.astuple())
+    assert on.tuning(1)["lookthrough"] == 1 and off.tuning(1)["lookthrough"] == 0
+    assert np.array_equal(_solve(on, b), ref)
+    assert np.array_equal(_solve(off, b), ref)
+    # FP32 storage and vectors: look-through equals the plain sweep and the FP32 oracle
+    on32 = _plan(monkeypatch, True, L.n, *L.astuple(), dtype="f32")
+    off32 = _plan(monkeypatch, False, L.n, *L.astuple(), dtype="f32")
+    r32 = b.astype(np.float32)
+    orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), r32)
+    got = _solve(on32, b, torch.float32)
+    assert np.array_equal(got, _solve(off32, b, torch.float32))
+    assert np.array_equal(got, r32)
+    # fused arithmetic: the two sweeps agree bit for bit
+    on.set_arith(ARITH_FUSED)
+    off.set_arith(ARITH_FUSED)
+    assert np.array_equal(_solve(on, b), _solve(off, b))
+
+
+def test_ilu_factors_and_transposed(gpu, orc, monkeypatch):
+    from sympiler_gb300._lib import ILU_UNIT_LOWER, ILU_UPPER, UPPER_DIAG_FIRST
+    C = mg.convdiff3d(20)
+    d = mg.diag_ptr(C)
+    lu, ok = orc.spilu0_csr(C.n, C.p, C.i, C.x, d)
+    assert ok
+    r = np.random.default_rng(6).uniform(-1, 1, C.n)
+    ref = orc.lus_cr(C.n, C.p, C.i, lu, d, r)  # unit-lower then upper with division
+    outs = []
+    for lt in (True, False):
+        Lu = _plan(monkeypatch, lt, C.n, C.p, C.i, lu, kind=ILU_UNIT_LOWER, diags=d)
+        Up = _plan(monkeypatch, lt, C.n, C.p, C.i, lu, kind=ILU_UPPER, diags=d)
+        x = torch.from_numpy(r.copy()).cuda()
+        Lu.solve(x)
+        Up.solve(x)
+        Up.check()
+        outs.append(x.cpu().numpy())
+    assert np.array_equal(outs[0], ref) and np.array_equal(outs[1], ref)
+    # the transposed solve of an IC0 factor (ltsolve's row form)
+    A = mg.lap3d(18, 1e-2)
+    U = mg.triu(A)
+    f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+    Lt = mg.CSR(U.n, U.p, U.i, f)  # CSC of L = CSR of L^T, diagonal first
+    b = np.random.default_rng(7).standard_normal(U.n)
+    ref = b.copy()
+    orc.ltsolve(U.n, *Lt.astuple(), ref)
+    for lt in (True, False):
+        P = _plan(monkeypatch, lt, U.n, *Lt.astuple(), kind=UPPER_DIAG_FIRST)
+        assert np.array_equal(_solve(P, b), ref)
+
+
+def test_wide_rows_fall_back_to_the_plain_sweep(gpu, orc, monkeypatch):
+    L = mg.random_lower(3000, 0.004, np.random.default_rng(8))
+    b = np.random.default_rng(9).uniform(-1, 1, L.n)
+    ref = b.copy()
+    orc.sptrsv_csr(L.n, *L.astuple(), ref)
+    P = _plan(monkeypatch, True, L.n, *L.astuple())
+    assert P.tuning(1)["lookthrough"] == 0  # rows of up to 22 entries
+    assert np.array_equal(_solve(P, b), ref)

@@ -317,7 +317,7 @@ def test_autotune_picks_a_working_executor(gpu, orc, c2_factor):
     chosen = plan.autotune(k=1)
     assert chosen in (1, 2, 3, 4, 5, 6)
     tun = plan.tuning(1)
-    assert tun["exec"] == chosen and tun["alt_lanes"] == 0
+    assert tun["exec"] == chosen and tun["lookthrough"] in (0, 1)
     assert tun["blocks_per_sm"] in (0, 1, 2, 3)
     b = np.random.default_rng(8).standard_normal(L.n)
     ref = b.copy()
