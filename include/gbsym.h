@@ -446,10 +446,12 @@ int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, int *chosen)
 /* The executor settings solves with k right-hand sides use (after
  * gbsym_tri_autotune, the tuned ones): tuning[0] the GBSYM_EXEC_*,
  * tuning[1] the sync-free sweep's blocks per SM (0: its default by k),
- * tuning[2] for k > 1 its lane layout (1: the alternative), for k = 1
- * whether it looks through one level (1: the spare lanes of each row
- * recompute its dependencies, so rows wait two levels back; plans whose
- * rows fit a three-entry slab).  No counterpart in the reference. */
+ * tuning[2] for k > 1 its lane layout in bit 0 (1: the alternative) and
+ * in bit 1 whether it looks through one level, for k = 1 whether it looks
+ * through (1).  Looking through, each row recomputes its dependencies'
+ * values (the spare lanes with one right-hand side, every lane for its own
+ * columns with several), so rows wait two levels back; plans whose rows
+ * fit a three-entry slab.  No counterpart in the reference. */
 int gbsym_tri_get_tuning(gbsym_tri t, int k, int *tuning);
 /* Waits for `stream` and returns the first error a device-side check of
  * this plan recorded since the last call (e.g. GBSYM_ERR_TIMEOUT from a

@@ -68,6 +68,7 @@ void choose_exec(gbsym_tri_s *t) {
   if (const char *sb = std::getenv("GBSYM_SF_BLOCKS_PER_SM")) t->sf_blocks_per_sm = std::atoi(sb);
   if (const char *al = std::getenv("GBSYM_SF_ALT_LANES")) t->sf_alt_lanes = std::atoi(al) == 1;
   if (const char *lt = std::getenv("GBSYM_SF_LOOKTHROUGH")) t->sf_lookthrough = std::atoi(lt) != 0;
+  if (const char *lm = std::getenv("GBSYM_SF_LT_MRHS")) t->sf_lt_mrhs = std::atoi(lm) != 0;
   t->sf_deal = num_sms();
   if (const char *sd = std::getenv("GBSYM_SF_DEAL")) t->sf_deal = std::atoi(sd);
 }
@@ -110,7 +111,8 @@ void tri_solve_into(gbsym_tri_s *t, const void *b, void *x, int k, int dtype, cu
   // sweep's scratch in packed row order, whose runs are contiguous, is
   // faster (C2 factor, one RHS: 236 us publishing into x against 212 us
   // for the copy and the in-place solve).
-  if (k >= 32 && effective_exec(t, k, false) == GBSYM_EXEC_SYNCFREE) {
+  if (k >= 32 && effective_exec(t, k, false) == GBSYM_EXEC_SYNCFREE &&
+      !(t->sf_lt_mrhs && sf_lookthrough_ok(t))) {
     if (dtype == GBSYM_F64) run_syncfree<double>(t, (double *)x, k, s, (const double *)b);
     else run_syncfree<float>(t, (float *)x, k, s, (const float *)b);
     return;
@@ -154,6 +156,10 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   // (bit 4) beside the plain one
   if (k == 1 && sf_lookthrough_ok(t))
     for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | 16});
+  // several right-hand sides: the look-through sweep (bit 5) where it may
+  // pay, a wavefront deeper than it is wide per lane group
+  if (k > 1 && sf_lookthrough_ok(t))
+    for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | 32});
   if (k == 1 && t->max_level_rows <= 4096) cands.push_back({GBSYM_EXEC_ONEBLOCK, 0});
   if (k == 1) {
     std::vector<int> sizes;
@@ -177,13 +183,18 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   const int saved_rows = t->part_rows_pref;
   const int kk = k > 1 ? 1 : 0;
   const int saved_bps = t->sf_bps_tuned[kk], saved_alt = t->sf_alt_lanes, saved_lt = t->sf_lookthrough;
+  const int saved_ltm = t->sf_lt_mrhs;
   for (const auto &cand : cands) {
     const int e = cand.first;
     if (e == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = cand.second;
     if (e == GBSYM_EXEC_SYNCFREE) {
       t->sf_bps_tuned[kk] = cand.second & 7;
-      if (k > 1) t->sf_alt_lanes = (cand.second >> 3) & 1;
-      else t->sf_lookthrough = (cand.second >> 4) & 1;
+      if (k > 1) {
+        t->sf_alt_lanes = (cand.second >> 3) & 1;
+        t->sf_lt_mrhs = (cand.second >> 5) & 1;
+      } else {
+        t->sf_lookthrough = (cand.second >> 4) & 1;
+      }
     }
     std::vector<float> ms;
     for (int rep = 0; rep < 4; ++rep) {
@@ -213,12 +224,17 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   t->sf_bps_tuned[kk] = saved_bps;
   t->sf_alt_lanes = saved_alt;
   t->sf_lookthrough = saved_lt;
+  t->sf_lt_mrhs = saved_ltm;
   if (best < 0) throw Err{GBSYM_ERR_TIMEOUT};
   if (best == GBSYM_EXEC_PARTITIONED) t->part_rows_pref = best_rows;
   if (best == GBSYM_EXEC_SYNCFREE) {
     t->sf_bps_tuned[kk] = best_rows & 7;
-    if (k > 1) t->sf_alt_lanes = (best_rows >> 3) & 1;
-    else t->sf_lookthrough = (best_rows >> 4) & 1;
+    if (k > 1) {
+      t->sf_alt_lanes = (best_rows >> 3) & 1;
+      t->sf_lt_mrhs = (best_rows >> 5) & 1;
+    } else {
+      t->sf_lookthrough = (best_rows >> 4) & 1;
+    }
   }
   if (k == 1) t->exec = best; else t->exec_mrhs = best;
   std::lock_guard<std::mutex> lk(g_tuned_mu);
@@ -255,7 +271,9 @@ extern "C" int gbsym_tri_get_tuning(gbsym_tri t, int k, int *tuning) {
   if (k < 1) return GBSYM_ERR_SIZE;
   tuning[0] = effective_exec(t, k, false);
   tuning[1] = t->sf_blocks_per_sm > 0 ? t->sf_blocks_per_sm : t->sf_bps_tuned[k > 1 ? 1 : 0];
-  tuning[2] = k > 1 ? t->sf_alt_lanes : (t->sf_lookthrough && sf_lookthrough_ok(t) ? 1 : 0);
+  const int lt_ok = sf_lookthrough_ok(t) ? 1 : 0;
+  tuning[2] = k > 1 ? (t->sf_alt_lanes | ((t->sf_lt_mrhs && lt_ok) ? 2 : 0))
+                    : (t->sf_lookthrough && lt_ok ? 1 : 0);
   return GBSYM_OK;
 }
 

@@ -142,6 +142,166 @@ k_syncfree_lt(TriView<T> A, T *x, T *y, const T *__restrict__ bp, const int *__r
   }
 }
 
+// ---- several right-hand sides ---------------------------------------------
+// Right-hand sides copied into packed row order (row-major n x k) and the
+// scratch set to the sentinel, in one pass.
+template <class T>
+__global__ void k_lt_prep_mrhs(int n, int k, const int *__restrict__ perm, const T *__restrict__ x,
+                               T *__restrict__ bp, T *__restrict__ y) {
+  const long long m = (long long)n * k;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
+       e += (long long)gridDim.x * blockDim.x) {
+    const long long row = e / k, c = e - row * k;
+    bp[e] = x[(long long)perm[row] * k + c];
+    if constexpr (sizeof(T) == 8) reinterpret_cast<unsigned long long *>(y)[e] = ~0ull;
+    else reinterpret_cast<unsigned *>(y)[e] = ~0u;
+  }
+}
+
+// G lanes per row, one value each, columns r = gl + s*G.  Every lane of a
+// row recomputes, for its own columns, the values of the row's dependencies
+// (from their rows, their right-hand sides and the values they depend on,
+// exactly as their owners compute them), then its row: it waits only for
+// values two levels back.  The arithmetic per value triples on stencil rows
+// of two or three entries; the sweep pays it where the publish -> poll hop,
+// not the arithmetic, bounds it (deep narrow wavefronts), and the autotuner
+// decides per plan.
+template <class T, int G, int AR, int KS>
+__global__ void __launch_bounds__(kSfBlock, KS <= 2 ? 3 : 2)
+k_syncfree_lt_mrhs(TriView<T> A, T *x, T *y, const T *__restrict__ bp, int k, const int *__restrict__ unit_row,
+                   const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int gl = lane % G;
+  const int sub = lane / G;
+  const int warp = deal_warp(nsm);
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int nslices = (k + G - 1) / G;
+  for (int u = warp; u < nunits; u += nwarps) {
+    const bool active = sub < unit_cnt[u];
+    const int row = unit_row[u] + sub;
+    RowStatic<T, KS> rs;
+    RowStatic<T, KS> ds[KS];
+    if (active) load_row(A, row, rs);
+    const int nq = active ? min(rs.len, A.K) : 0;
+#pragma unroll
+    for (int q = 0; q < KS; ++q)
+      if (q < nq) load_row(A, rs.c[q], ds[q]);
+    for (int sl = 0; sl < nslices; ++sl) {
+      const int r = gl + sl * G;
+      const bool live = active && r < k;
+      T acc = live ? bp[(size_t)row * k + r] : T(0);
+      T aq[KS], xv[KS][KS];
+      unsigned got = 0, need = 0;
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (live && q < nq) {
+          aq[q] = bp[(size_t)rs.c[q] * k + r];
+#pragma unroll
+          for (int m = 0; m < KS; ++m)
+            if (m < min(ds[q].len, A.K)) need |= 1u << (q * KS + m);
+        }
+      bool done = !live || need == 0;
+      long long t0 = clock_now();
+      int rounds = 0;
+      while (__any_sync(FULL, !done)) {
+        bool moved = false;
+        if (!done) {
+#pragma unroll
+          for (int q = 0; q < KS; ++q)
+#pragma unroll
+            for (int m = 0; m < KS; ++m)
+              if (((need & ~got) >> (q * KS + m)) & 1u) {
+                T v[1];
+                ld_rlx<T, 1>(y + (size_t)ds[q].c[m] * k + r, v);
+                xv[q][m] = v[0];  // a value already seen is never loaded again
+              }
+#pragma unroll
+          for (int q = 0; q < KS; ++q)
+#pragma unroll
+            for (int m = 0; m < KS; ++m)
+              if ((((need & ~got) >> (q * KS + m)) & 1u) && !is_sentinel(xv[q][m])) {
+                got |= 1u << (q * KS + m);
+                moved = true;
+              }
+          if (got == need) done = true;
+          if (moved) t0 = clock_now();
+        }
+        if (!__any_sync(FULL, moved)) __nanosleep(32);
+        if ((++rounds & 63) == 0) {
+          if (!done && clock_now() - t0 > kWaitLimitCycles) {
+            atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
+            done = true;
+          }
+          const int e = lane == 0 ? ld_relaxed(err) : 0;
+          if (__shfl_sync(FULL, e, 0) != 0) return;
+        }
+      }
+      if (live) {
+        T xq[KS];
+#pragma unroll
+        for (int q = 0; q < KS; ++q)
+          if (q < nq) {
+            T a = aq[q];
+#pragma unroll
+            for (int m = 0; m < KS; ++m)
+              if (m < min(ds[q].len, A.K)) a = msub<AR>(a, ds[q].v[m], xv[q][m]);
+            xq[q] = row_finish(A, ds[q], a);
+          }
+#pragma unroll
+        for (int q = 0; q < KS; ++q)
+          if (q < nq) acc = msub<AR>(acc, rs.v[q], xq[q]);
+        const T out = row_finish(A, rs, acc);
+        x[(size_t)rs.orig * k + r] = out;
+        T o[1] = {not_sentinel(out)};
+        st_rlx<T, 1>(y + (size_t)row * k + r, o);
+      }
+    }
+  }
+}
+
+template <class T, int G, int AR, int KS>
+static void lt_mrhs_launch(gbsym_tri_s *t, T *x, T *y, const T *bp, int k, cudaStream_t s) {
+  const TriView<T> A = view_packed_of<T>(t);
+  const Units U = sf_units(t, 32 / G);
+  launch_coop(t, k, k_syncfree_lt_mrhs<T, G, AR, KS>, s, A, x, y, bp, k, U.row, U.cnt, U.n, t->sf_deal,
+              t->err.p);
+}
+
+template <class T, int AR, int KS>
+static void lt_mrhs_g(gbsym_tri_s *t, T *x, T *y, const T *bp, int k, cudaStream_t s) {
+  if (k <= 2) lt_mrhs_launch<T, 2, AR, KS>(t, x, y, bp, k, s);
+  else if (k <= 4) lt_mrhs_launch<T, 4, AR, KS>(t, x, y, bp, k, s);
+  else if (k <= 8) lt_mrhs_launch<T, 8, AR, KS>(t, x, y, bp, k, s);
+  else if (k <= 16) lt_mrhs_launch<T, 16, AR, KS>(t, x, y, bp, k, s);
+  else lt_mrhs_launch<T, 32, AR, KS>(t, x, y, bp, k, s);
+}
+
+template <class T>
+void run_syncfree_lt_mrhs(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
+  GB_CHECK(t->K <= 3 && t->nov == 0 && k >= 1, GBSYM_ERR_UNSUPPORTED);
+  const size_t bytes = (size_t)t->n * k * sizeof(T);
+  t->sfy.reserve(bytes);
+  t->sfb.reserve(bytes);
+  T *y = reinterpret_cast<T *>(t->sfy.p);
+  T *bp = reinterpret_cast<T *>(t->sfb.p);
+  const long long m = (long long)t->n * k;
+  const int grid = (int)std::max<long long>(1, std::min<long long>(div_up(m, 256LL), num_sms() * 8LL));
+  k_lt_prep_mrhs<T><<<grid, 256, 0, s>>>(t->n, k, t->perm.p, x, bp, y);
+  check_launch();
+  const bool fused = t->arith == kArithFused;
+  if (t->K <= 2) {
+    if (fused) lt_mrhs_g<T, kArithFused, 2>(t, x, y, bp, k, s);
+    else lt_mrhs_g<T, kArithExact, 2>(t, x, y, bp, k, s);
+  } else {
+    if (fused) lt_mrhs_g<T, kArithFused, 3>(t, x, y, bp, k, s);
+    else lt_mrhs_g<T, kArithExact, 3>(t, x, y, bp, k, s);
+  }
+}
+
+template void run_syncfree_lt_mrhs<double>(gbsym_tri_s *, double *, int, cudaStream_t);
+template void run_syncfree_lt_mrhs<float>(gbsym_tri_s *, float *, int, cudaStream_t);
+
 template <class T, int AR, int KS>
 static void lt_launch(gbsym_tri_s *t, T *x, T *y, const T *bp, cudaStream_t s) {
   const TriView<T> A = view_packed_of<T>(t);

@@ -55,6 +55,10 @@ void run_syncfree(gbsym_tri_s *t, T *x, int k, cudaStream_t s, const T *b) {
     run_syncfree_lt<T>(t, x, s);
     return;
   }
+  if (k > 1 && !b && t->sf_lt_mrhs && sf_lookthrough_ok(t)) {
+    run_syncfree_lt_mrhs<T>(t, x, k, s);
+    return;
+  }
   const size_t bytes = (size_t)t->n * k * sizeof(T);
   T *y = x;
   if (!b) {

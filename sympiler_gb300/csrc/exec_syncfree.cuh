@@ -31,5 +31,8 @@ void sf_run_ks(gbsym_tri_s *t, T *x, T *y, const T *b, int k, cudaStream_t s);
 inline bool sf_lookthrough_ok(const gbsym_tri_s *t) { return t->K <= 3 && t->nov == 0; }
 template <class T>
 void run_syncfree_lt(gbsym_tri_s *t, T *x, cudaStream_t s);
+// k > 1 right-hand sides, in place, with look-through (exec_sf_lt.cu)
+template <class T>
+void run_syncfree_lt_mrhs(gbsym_tri_s *t, T *x, int k, cudaStream_t s);
 
 }  // namespace gbsym

@@ -99,6 +99,8 @@ struct gbsym_tri_s {
   int sf_lookthrough = 1;            // k = 1: spare lanes recompute each row's dependencies, so
                                      // rows wait two levels back (exec_sf_lt.cu); plans whose
                                      // rows fit a three-entry slab, 0: the plain sweep
+  int sf_lt_mrhs = 0;                // k > 1: the look-through sweep for several right-hand
+                                     // sides (the autotuner's choice; in place only)
   struct PartPlan {
     int R = 0, nparts = 0, ngroups = 0;  // rows per partition (0: not built)
     gbsym::DBuf<int> part_group, group_ptr, rows;

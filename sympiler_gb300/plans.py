@@ -113,7 +113,9 @@ class TriPlan:
         layout (alt_lanes), for k = 1 the look-through sweep (lookthrough)."""
         v = (C.c_int * 3)()
         check(lib().gbsym_tri_get_tuning(self._h, int(k), v), "gbsym_tri_get_tuning")
-        return {"exec": v[0], "blocks_per_sm": v[1], ("alt_lanes" if k > 1 else "lookthrough"): v[2]}
+        if k > 1:
+            return {"exec": v[0], "blocks_per_sm": v[1], "alt_lanes": v[2] & 1, "lookthrough": (v[2] >> 1) & 1}
+        return {"exec": v[0], "blocks_per_sm": v[1], "lookthrough": v[2]}
 
     def schedule(self):
         inf = self.info()
@@ -381,7 +383,9 @@ class BatchPlan:
         """Executor settings used for k right-hand sides (gbsym_batch_get_tuning)."""
         v = (C.c_int * 3)()
         check(lib().gbsym_batch_get_tuning(self._h, int(k), v), "gbsym_batch_get_tuning")
-        return {"exec": v[0], "blocks_per_sm": v[1], ("alt_lanes" if k > 1 else "lookthrough"): v[2]}
+        if k > 1:
+            return {"exec": v[0], "blocks_per_sm": v[1], "alt_lanes": v[2] & 1, "lookthrough": (v[2] >> 1) & 1}
+        return {"exec": v[0], "blocks_per_sm": v[1], "lookthrough": v[2]}
 
     def autotune(self, k=1, dtype=None, stream=None) -> int:
         """Time the executors on the batch for k right-hand sides; returns the chosen one."""

@@ -99,3 +99,44 @@ def test_wide_rows_fall_back_to_the_plain_sweep(gpu, orc, monkeypatch):
     P = _plan(monkeypatch, True, L.n, *L.astuple())
     assert P.tuning(1)["lookthrough"] == 0  # rows of up to 22 entries
     assert np.array_equal(_solve(P, b), ref)
+
+
+@pytest.mark.parametrize("k", [3, 8, 40])
+@pytest.mark.parametrize("dtype", ["f64", "f32"])
+def test_several_rhs_lookthrough(gpu, orc, monkeypatch, k, dtype):
+    """The look-through sweep for several right-hand sides (every lane
+    recomputes the row's dependencies for its own columns), in place and
+    through the out-of-place entry, against the plain sweep and the oracle."""
+    from sympiler_gb300._lib import LOWER_CSC
+    from sympiler_gb300.plans import TriPlan
+    for A in (mg.lap2d(40, 30), mg.lap3d(14, 1e-2)):
+        U = mg.triu(A)
+        f, ok = orc.spic0_csr(U.n, U.p, U.i, U.x)
+        assert ok
+        tdt = torch.float64 if dtype == "f64" else torch.float32
+        B = np.random.default_rng(k).standard_normal((U.n, k))
+        plans = []
+        for lt in ("1", "0"):
+            monkeypatch.setenv("GBSYM_SF_LT_MRHS", lt)
+            P = TriPlan(U.n, U.p, U.i, f, kind=LOWER_CSC, dtype=dtype)
+            monkeypatch.delenv("GBSYM_SF_LT_MRHS")
+            from sympiler_gb300._lib import EXEC_SYNCFREE
+            P.set_exec(EXEC_SYNCFREE)
+            plans.append(P)
+        assert plans[0].tuning(k)["lookthrough"] == 1 and plans[1].tuning(k)["lookthrough"] == 0
+        outs = []
+        for P in plans:
+            X = torch.from_numpy(B.copy()).to(tdt).cuda()
+            P.solve(X)
+            P.check()
+            Y = torch.empty_like(X)
+            P.solve_into(torch.from_numpy(B.copy()).to(tdt).cuda(), Y)
+            P.check()
+            assert torch.equal(X, Y)
+            outs.append(X.cpu().numpy())
+        assert np.array_equal(outs[0], outs[1])
+        if dtype == "f64":
+            for c in (0, k - 1):
+                col = B[:, c].copy()
+                orc.sptrsv_csc(U.n, U.p, U.i, f, col)
+                assert np.array_equal(outs[0][:, c], col)
