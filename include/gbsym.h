@@ -447,10 +447,11 @@ int gbsym_tri_autotune(gbsym_tri t, int k, int dtype, void *stream, int *chosen)
  * gbsym_tri_autotune, the tuned ones): tuning[0] the GBSYM_EXEC_*,
  * tuning[1] the sync-free sweep's blocks per SM (0: its default by k),
  * tuning[2] for k > 1 its lane layout in bit 0 (1: the alternative) and
- * in bit 1 whether it looks through one level, for k = 1 whether it looks
- * through (1).  Looking through, each row recomputes its dependencies'
- * values (the spare lanes with one right-hand side, every lane for its own
- * columns with several), so rows wait two levels back; plans whose rows
+ * in bit 1 whether it looks through one level, for k = 1 how many levels it
+ * looks through (0, 1 or 2).  Looking through, each row recomputes its
+ * dependencies' values (the spare lanes with one right-hand side -- and
+ * with two levels their dependencies' too -- every lane for its own columns
+ * with several), so rows wait two (three) levels back; plans whose rows
  * fit a three-entry slab.  No counterpart in the reference. */
 int gbsym_tri_get_tuning(gbsym_tri t, int k, int *tuning);
 /* Waits for `stream` and returns the first error a device-side check of

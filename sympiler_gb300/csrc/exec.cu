@@ -67,7 +67,7 @@ void choose_exec(gbsym_tri_s *t) {
   if (const char *cb = std::getenv("GBSYM_CLUSTER_BLOCKS")) t->cluster_blocks = std::atoi(cb);
   if (const char *sb = std::getenv("GBSYM_SF_BLOCKS_PER_SM")) t->sf_blocks_per_sm = std::atoi(sb);
   if (const char *al = std::getenv("GBSYM_SF_ALT_LANES")) t->sf_alt_lanes = std::atoi(al) == 1;
-  if (const char *lt = std::getenv("GBSYM_SF_LOOKTHROUGH")) t->sf_lookthrough = std::atoi(lt) != 0;
+  if (const char *lt = std::getenv("GBSYM_SF_LOOKTHROUGH")) t->sf_lookthrough = std::max(0, std::min(2, std::atoi(lt)));
   if (const char *lm = std::getenv("GBSYM_SF_LT_MRHS")) t->sf_lt_mrhs = std::atoi(lm) != 0;
   t->sf_deal = num_sms();
   if (const char *sd = std::getenv("GBSYM_SF_DEAL")) t->sf_deal = std::atoi(sd);
@@ -153,9 +153,10 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
   if (k > 1)
     for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | 8});
   // one right-hand side on a plan that allows it: the look-through sweep
-  // (bit 4) beside the plain one
+  // over one level (bits 4-5 = 1) and over two (= 2) beside the plain one
   if (k == 1 && sf_lookthrough_ok(t))
-    for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | 16});
+    for (int lv = 1; lv <= 2; ++lv)
+      for (int b = 1; b <= 3; ++b) cands.push_back({GBSYM_EXEC_SYNCFREE, b | (lv << 4)});
   // several right-hand sides: the look-through sweep (bit 5) where it may
   // pay, a wavefront deeper than it is wide per lane group
   if (k > 1 && sf_lookthrough_ok(t))
@@ -193,7 +194,7 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
         t->sf_alt_lanes = (cand.second >> 3) & 1;
         t->sf_lt_mrhs = (cand.second >> 5) & 1;
       } else {
-        t->sf_lookthrough = (cand.second >> 4) & 1;
+        t->sf_lookthrough = (cand.second >> 4) & 3;
       }
     }
     std::vector<float> ms;
@@ -233,7 +234,7 @@ static int autotune_typed(gbsym_tri_s *t, int k, int dtype, cudaStream_t s) {
       t->sf_alt_lanes = (best_rows >> 3) & 1;
       t->sf_lt_mrhs = (best_rows >> 5) & 1;
     } else {
-      t->sf_lookthrough = (best_rows >> 4) & 1;
+      t->sf_lookthrough = (best_rows >> 4) & 3;
     }
   }
   if (k == 1) t->exec = best; else t->exec_mrhs = best;
@@ -273,7 +274,7 @@ extern "C" int gbsym_tri_get_tuning(gbsym_tri t, int k, int *tuning) {
   tuning[1] = t->sf_blocks_per_sm > 0 ? t->sf_blocks_per_sm : t->sf_bps_tuned[k > 1 ? 1 : 0];
   const int lt_ok = sf_lookthrough_ok(t) ? 1 : 0;
   tuning[2] = k > 1 ? (t->sf_alt_lanes | ((t->sf_lt_mrhs && lt_ok) ? 2 : 0))
-                    : (t->sf_lookthrough && lt_ok ? 1 : 0);
+                    : (lt_ok ? t->sf_lookthrough : 0);
   return GBSYM_OK;
 }
 

@@ -142,6 +142,146 @@ k_syncfree_lt(TriView<T> A, T *x, T *y, const T *__restrict__ bp, const int *__r
   }
 }
 
+// ---- one right-hand side, two levels ----------------------------------------
+// Sixteen lanes per row (two rows per warp unit): lane 0 the row, lanes
+// 1..3 its dependencies j, lanes 4..12 the dependencies of those (lane
+// 4 + 3q + m: dependency m of dependency q).  The outer lanes poll values
+// three levels back and recompute their rows, the middle lanes rebuild the
+// dependencies from those, lane 0 its row: each publish -> poll hop then
+// advances the wavefront three levels, for three dependent row chains.
+template <class T, int AR, int KS>
+__global__ void __launch_bounds__(kSfBlock, 3)
+k_syncfree_lt2(TriView<T> A, T *x, T *y, const T *__restrict__ bp, const int *__restrict__ unit_row,
+               const int *__restrict__ unit_cnt, int nunits, int nsm, int *err) {
+  constexpr unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int gl = lane & 15;
+  const int sub = lane >> 4;
+  const int base = lane & 16;
+  const int warp = deal_warp(nsm);
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  const int q1 = gl >= 4 ? (gl - 4) / 3 : gl - 1;  // dependency of the row this lane follows
+  const int m2 = gl >= 4 ? (gl - 4) % 3 : 0;       // outer lanes: dependency of that dependency
+  for (int u = warp; u < nunits; u += nwarps) {
+    const bool active = sub < unit_cnt[u];
+    const int row = unit_row[u] + sub;
+    const int rlen = active ? min(A.len[row], A.K) : 0;
+    int me = row;
+    bool work = active && gl <= 12;
+    if (work && gl > 0) {
+      if (q1 < rlen) {
+        me = A.sci[(size_t)q1 * A.npad + row];
+        if (gl >= 4) {
+          const int l1 = min(A.len[me], A.K);
+          if (m2 < l1) me = A.sci[(size_t)m2 * A.npad + me];
+          else work = false;
+        }
+      } else {
+        work = false;
+      }
+    }
+    RowStatic<T, KS> rs;
+    if (work) load_row(A, me, rs);
+    T acc = work ? bp[me] : T(0);
+    const bool outer = work && gl >= 4;
+    const int ns = outer ? min(rs.len, A.K) : 0;
+    const unsigned need = (1u << ns) - 1u;
+    unsigned got = 0;
+    T xv[KS], va[KS], vb[KS];
+    bool done = !outer || ns == 0;
+    auto issue = [&](T (&buf)[KS]) {
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < ns && !((got >> q) & 1u)) {
+          T v[1];
+          ld_rlx<T, 1>(y + rs.c[q], v);
+          buf[q] = v[0];
+        }
+    };
+    auto absorb = [&](T (&buf)[KS]) {
+      bool moved = false;
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < ns && !((got >> q) & 1u) && !is_sentinel(buf[q])) {
+          xv[q] = buf[q];
+          got |= 1u << q;
+          moved = true;
+        }
+      if (got == need) done = true;
+      return moved;
+    };
+    if (!done) issue(va);
+    long long t0 = clock_now();
+    int rounds = 0;
+    bool odd = false;
+    while (__any_sync(FULL, !done)) {
+      bool moved = false;
+      if (!done) {
+        if (!odd) {
+          issue(vb);
+          moved = absorb(va);
+        } else {
+          issue(va);
+          moved = absorb(vb);
+        }
+        if (moved) t0 = clock_now();
+      }
+      odd = !odd;
+      if (!__any_sync(FULL, moved)) __nanosleep(32);
+      if ((++rounds & 63) == 0) {
+        if (!done && clock_now() - t0 > kWaitLimitCycles) {
+          atomicCAS(err, 0, GBSYM_ERR_TIMEOUT);
+          done = true;
+        }
+        const int e = lane == 0 ? ld_relaxed(err) : 0;
+        if (__shfl_sync(FULL, e, 0) != 0) return;
+      }
+    }
+    // outer lanes: their rows from polled values
+    T v2 = T(0);
+    if (outer) {
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < ns) acc = msub<AR>(acc, rs.v[q], xv[q]);
+      v2 = row_finish(A, rs, acc);
+    }
+    // middle lanes (1..3): their rows from the outer lanes' values
+    const int src2 = (gl >= 1 && gl <= 3) ? base + 4 + 3 * (gl - 1) : lane;
+    T d2[3];
+    d2[0] = __shfl_sync(FULL, v2, src2);
+    d2[1] = __shfl_sync(FULL, v2, gl >= 1 && gl <= 3 ? src2 + 1 : lane);
+    d2[2] = __shfl_sync(FULL, v2, gl >= 1 && gl <= 3 ? src2 + 2 : lane);
+    T v1 = T(0);
+    if (work && gl >= 1 && gl <= 3) {
+      const int l1 = min(rs.len, A.K);
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < l1) acc = msub<AR>(acc, rs.v[q], d2[q]);
+      v1 = row_finish(A, rs, acc);
+    }
+    T d1[3];
+    d1[0] = __shfl_sync(FULL, v1, base + 1);
+    d1[1] = __shfl_sync(FULL, v1, base + 2);
+    d1[2] = __shfl_sync(FULL, v1, base + 3);
+    if (work && gl == 0) {
+#pragma unroll
+      for (int q = 0; q < KS; ++q)
+        if (q < rlen) acc = msub<AR>(acc, rs.v[q], d1[q]);
+      const T out = row_finish(A, rs, acc);
+      x[rs.orig] = out;
+      T o[1] = {not_sentinel(out)};
+      st_rlx<T, 1>(y + row, o);
+    }
+  }
+}
+
+template <class T, int AR, int KS>
+static void lt2_launch(gbsym_tri_s *t, T *x, T *y, const T *bp, cudaStream_t s) {
+  const TriView<T> A = view_packed_of<T>(t);
+  const Units U = sf_units(t, 2);
+  launch_coop(t, 1, k_syncfree_lt2<T, AR, KS>, s, A, x, y, bp, U.row, U.cnt, U.n, t->sf_deal, t->err.p);
+}
+
 // ---- several right-hand sides ---------------------------------------------
 // Right-hand sides copied into packed row order (row-major n x k) and the
 // scratch set to the sentinel, in one pass.
@@ -321,6 +461,16 @@ void run_syncfree_lt(gbsym_tri_s *t, T *x, cudaStream_t s) {
   k_lt_prep<T><<<grid, 256, 0, s>>>(t->n, t->perm.p, x, bp, y);
   check_launch();
   const bool fused = t->arith == kArithFused;
+  if (t->sf_lookthrough == 2) {
+    if (t->K <= 2) {
+      if (fused) lt2_launch<T, kArithFused, 2>(t, x, y, bp, s);
+      else lt2_launch<T, kArithExact, 2>(t, x, y, bp, s);
+    } else {
+      if (fused) lt2_launch<T, kArithFused, 3>(t, x, y, bp, s);
+      else lt2_launch<T, kArithExact, 3>(t, x, y, bp, s);
+    }
+    return;
+  }
   if (t->K <= 2) {
     if (fused) lt_launch<T, kArithFused, 2>(t, x, y, bp, s);
     else lt_launch<T, kArithExact, 2>(t, x, y, bp, s);

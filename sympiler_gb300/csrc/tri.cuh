@@ -96,9 +96,10 @@ struct gbsym_tri_s {
   int sf_alt_lanes = 0;              // k > 1, 1: the other lane layout (FP64: two values per
                                      // lane; FP32: two), the autotuner's choice
   int sf_deal = 0;                   // sync-free unit dealing: SM count to spread over (0: plain order)
-  int sf_lookthrough = 1;            // k = 1: spare lanes recompute each row's dependencies, so
-                                     // rows wait two levels back (exec_sf_lt.cu); plans whose
-                                     // rows fit a three-entry slab, 0: the plain sweep
+  int sf_lookthrough = 1;            // k = 1: spare lanes recompute each row's dependencies (1),
+                                     // and theirs (2), so rows wait two (three) levels back
+                                     // (exec_sf_lt.cu); plans whose rows fit a three-entry slab;
+                                     // 0: the plain sweep
   int sf_lt_mrhs = 0;                // k > 1: the look-through sweep for several right-hand
                                      // sides (the autotuner's choice; in place only)
   struct PartPlan {

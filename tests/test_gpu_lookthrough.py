@@ -1,5 +1,6 @@
-"""The one-right-hand-side look-through sweep (spare lanes recompute each
-row's dependencies so that rows wait two levels back) against the plain
+"""The look-through sweeps (spare lanes recompute each row's dependencies,
+and with two levels theirs, so that rows wait two or three levels back;
+for several right-hand sides every lane does so for its columns) against the plain
 sync-free sweep and the oracle, bit for bit, for every row form it serves:
 lower CSR with the diagonal last, unit lower and upper ILU factors, the
 transposed (upper) solve, FP64 and FP32, exact and fused arithmetic.  Plans
@@ -16,7 +17,7 @@ pytestmark = pytest.mark.gpu
 def _plan(monkeypatch, lookthrough, *args, **kw):
     from sympiler_gb300._lib import EXEC_SYNCFREE
     from sympiler_gb300.plans import TriPlan
-    monkeypatch.setenv("GBSYM_SF_LOOKTHROUGH", "1" if lookthrough else "0")
+    monkeypatch.setenv("GBSYM_SF_LOOKTHROUGH", str(int(lookthrough)))
     P = TriPlan(*args, **kw)
     monkeypatch.delenv("GBSYM_SF_LOOKTHROUGH")
     P.set_exec(EXEC_SYNCFREE)
@@ -30,8 +31,9 @@ def _solve(P, b, dtype=torch.float64):
     return x.cpu().numpy()
 
 
+@pytest.mark.parametrize("levels", [1, 2])
 @pytest.mark.parametrize("grid", [(60, 50), (24, 20, 16)])
-def test_lower_fp64_fp32_exact_and_fused(gpu, orc, monkeypatch, grid):
+def test_lower_fp64_fp32_exact_and_fused(gpu, orc, monkeypatch, grid, levels):
     from sympiler_gb300._lib import ARITH_FUSED
     A = mg.lap2d(*grid) if len(grid) == 2 else mg.lap3d(grid[0], 1e-2)
     U = mg.triu(A)
@@ -41,14 +43,14 @@ def test_lower_fp64_fp32_exact_and_fused(gpu, orc, monkeypatch, grid):
     b = np.random.default_rng(5).standard_normal(L.n)
     ref = b.copy()
     orc.sptrsv_csr(L.n, *L.astuple(), ref)
-    on = _plan(monkeypatch, True, L.n, *L.astuple())
-    off = _plan(monkeypatch, False, L.n, *L.astuple())
-    assert on.tuning(1)["lookthrough"] == 1 and off.tuning(1)["lookthrough"] == 0
+    on = _plan(monkeypatch, levels, L.n, *L.astuple())
+    off = _plan(monkeypatch, 0, L.n, *L.astuple())
+    assert on.tuning(1)["lookthrough"] == levels and off.tuning(1)["lookthrough"] == 0
     assert np.array_equal(_solve(on, b), ref)
     assert np.array_equal(_solve(off, b), ref)
     # FP32 storage and vectors: look-through equals the plain sweep and the FP32 oracle
-    on32 = _plan(monkeypatch, True, L.n, *L.astuple(), dtype="f32")
-    off32 = _plan(monkeypatch, False, L.n, *L.astuple(), dtype="f32")
+    on32 = _plan(monkeypatch, levels, L.n, *L.astuple(), dtype="f32")
+    off32 = _plan(monkeypatch, 0, L.n, *L.astuple(), dtype="f32")
     r32 = b.astype(np.float32)
     orc.sptrsv_csr_f32(L.n, L.p, L.i, L.x.astype(np.float32), r32)
     got = _solve(on32, b, torch.float32)
@@ -60,7 +62,8 @@ def test_lower_fp64_fp32_exact_and_fused(gpu, orc, monkeypatch, grid):
     assert np.array_equal(_solve(on, b), _solve(off, b))
 
 
-def test_ilu_factors_and_transposed(gpu, orc, monkeypatch):
+@pytest.mark.parametrize("levels", [1, 2])
+def test_ilu_factors_and_transposed(gpu, orc, monkeypatch, levels):
     from sympiler_gb300._lib import ILU_UNIT_LOWER, ILU_UPPER, UPPER_DIAG_FIRST
     C = mg.convdiff3d(20)
     d = mg.diag_ptr(C)
@@ -69,7 +72,7 @@ def test_ilu_factors_and_transposed(gpu, orc, monkeypatch):
     r = np.random.default_rng(6).uniform(-1, 1, C.n)
     ref = orc.lus_cr(C.n, C.p, C.i, lu, d, r)  # unit-lower then upper with division
     outs = []
-    for lt in (True, False):
+    for lt in (levels, 0):
         Lu = _plan(monkeypatch, lt, C.n, C.p, C.i, lu, kind=ILU_UNIT_LOWER, diags=d)
         Up = _plan(monkeypatch, lt, C.n, C.p, C.i, lu, kind=ILU_UPPER, diags=d)
         x = torch.from_numpy(r.copy()).cuda()
@@ -86,7 +89,7 @@ def test_ilu_factors_and_transposed(gpu, orc, monkeypatch):
     b = np.random.default_rng(7).standard_normal(U.n)
     ref = b.copy()
     orc.ltsolve(U.n, *Lt.astuple(), ref)
-    for lt in (True, False):
+    for lt in (levels, 0):
         P = _plan(monkeypatch, lt, U.n, *Lt.astuple(), kind=UPPER_DIAG_FIRST)
         assert np.array_equal(_solve(P, b), ref)
 
@@ -96,7 +99,7 @@ def test_wide_rows_fall_back_to_the_plain_sweep(gpu, orc, monkeypatch):
     b = np.random.default_rng(9).uniform(-1, 1, L.n)
     ref = b.copy()
     orc.sptrsv_csr(L.n, *L.astuple(), ref)
-    P = _plan(monkeypatch, True, L.n, *L.astuple())
+    P = _plan(monkeypatch, 1, L.n, *L.astuple())
     assert P.tuning(1)["lookthrough"] == 0  # rows of up to 22 entries
     assert np.array_equal(_solve(P, b), ref)
 
