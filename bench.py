@@ -11,9 +11,12 @@ synthetic data of the named shape.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gbsym|reference]
 
-Under torchrun each rank solves its own replica (the path does not shard
-across GPUs for one system: "replicas only"); value is the sum over ranks
-of the per-rank throughput measured over the max-over-ranks time.
+Under torchrun each rank solves its own replica (one system's rows do not
+shard across GPUs: "replicas"); value is the sum over ranks of the per-rank
+throughput measured over the max-over-ranks time.  With --shard rhs the
+right-hand-side columns of one solve are split over the ranks instead,
+each rank holding the factor (strong scaling, no collective on the data
+path).
 
 --impl reference times the reference's CPU executor for the same workload
 on the host cores: the oracle's C restatement of sptrsv_csr_levelset
@@ -56,6 +59,9 @@ def parse():
                     help="c2: one IC0 forward solve with --rhs right-hand sides (default); c4: the 512-system "
                          "batch, sharded over the ranks")
     ap.add_argument("--dtype", default="f64", choices=["f64", "f32"], help="c4 workload: factor and vectors")
+    ap.add_argument("--shard", default="replicas", choices=["replicas", "rhs"],
+                    help="c2 workload under torchrun: replicas (each rank solves all columns) or rhs "
+                         "(the columns split over the ranks, each rank holding the whole factor)")
     ap.add_argument("--exec", default="auto",
                     choices=["auto", "levelset", "syncfree", "oneblock", "persistent", "cluster", "partitioned"],
                     help="force one executor instead of autotuning (profiling runs)")
@@ -945,7 +951,14 @@ def main():
     from sympiler_gb300._lib import UPPER_DIAG_FIRST
     from sympiler_gb300.plans import CsrPlan, TriPlan
 
-    k = args.rhs
+    k_all = args.rhs
+    shard_rhs = args.shard == "rhs" and world > 1
+    if shard_rhs:
+        from sympiler_gb300.shard import column_range
+        c0, c1 = column_range(k_all, rank, world)
+    else:
+        c0, c1 = 0, k_all
+    k = c1 - c0  # this rank's right-hand sides
     g = args.grid
     A = mg.lap3d(g, 1e-2)
     U = mg.triu(A)
@@ -967,8 +980,10 @@ def main():
     n = L.n
     byt = algorithmic_bytes(L.nnz, n, k)
 
-    rng = np.random.default_rng(1234 + rank)
-    B = torch.from_numpy(rng.standard_normal((n, k))).to(dev)
+    if shard_rhs:  # one problem, its columns split: every rank draws the same B
+        B = torch.from_numpy(np.random.default_rng(1234).standard_normal((n, k_all))[:, c0:c1].copy()).to(dev)
+    else:
+        B = torch.from_numpy(np.random.default_rng(1234 + rank).standard_normal((n, k))).to(dev)
     X = torch.empty_like(B)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
     stream = torch.cuda.current_stream()
@@ -1015,6 +1030,10 @@ def main():
             t_step = float(tt.item())
         value_rank = byt / t_step / 1e9
         value = value_rank * world
+        if shard_rhs:  # every rank's bytes (its factor copy and its columns) over the slowest rank's time
+            bt = torch.tensor([float(byt)], dtype=torch.float64, device=dev)
+            torch.distributed.all_reduce(bt)
+            value = float(bt.item()) / t_step / 1e9
 
         # end to end through the C ABI on pinned host buffers.  On a coherent
         # CPU-GPU system the library solves such a buffer in place over the
@@ -1070,8 +1089,12 @@ def main():
         result.update({
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_step * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": dict(config(g, k), levels=info.levels, nnz_L=int(L.nnz), executor=tuned,
+            "scaling": "strong" if shard_rhs else "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": dict(config(g, k_all), levels=info.levels, nnz_L=int(L.nnz), executor=tuned,
+                           parallelism=("%d RHS columns split over %d ranks (this rank: %d..%d), each rank "
+                                        "holding the factor; no collective on the data path"
+                                        % (k_all, world, c0, c1) if shard_rhs else "replicas"),
                            arithmetic="exact (reference operation order, bit-identical)",
                            api="gbsym_tri_solve_into: X = L^-1 B out of place, B unchanged",
                            wall_s_timed_region=wall),

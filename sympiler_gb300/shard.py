@@ -1,7 +1,10 @@
-"""Placement of independent systems on the ranks of a multi-GPU run.
+"""Placement of independent work on the ranks of a multi-GPU run.
 
-A single triangular solve does not shard (every level depends on all the
-levels before it), so one system runs as a replica per GPU.  A batch of
+A single triangular solve does not shard along its rows (every level
+depends on all the levels before it), so one system with one right-hand
+side runs as a replica per GPU.  Its right-hand-side columns do shard: each
+rank can solve a block of them against its own copy of the factor
+(column_range).  A batch of
 independent systems does: each rank takes a subset and solves it with its
 own batched plan, and no data crosses ranks (no collective on the data
 path).  Systems are placed by longest-processing-time-first greedy bin
@@ -35,6 +38,18 @@ def partition_systems(costs: Sequence[int], world: int) -> List[List[int]]:
 
 def rank_systems(costs: Sequence[int], rank: int, world: int) -> List[int]:
     return partition_systems(costs, world)[rank]
+
+
+def column_range(k: int, rank: int, world: int):
+    """The contiguous block of right-hand-side columns [start, stop) a rank
+    solves when the k columns of one solve are split over the ranks: every
+    rank reads the whole factor, the columns are independent, and the sizes
+    differ by at most one."""
+    if world < 1 or not 0 <= rank < world:
+        raise ValueError("need 0 <= rank < world")
+    base, extra = divmod(int(k), world)
+    start = rank * base + min(rank, extra)
+    return start, start + base + (1 if rank < extra else 0)
 
 
 def shard_systems(systems: Sequence, rank: int, world: int):

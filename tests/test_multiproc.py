@@ -14,7 +14,7 @@ import torch.distributed as dist
 import torch.multiprocessing as mp
 
 from sympiler_gb300 import matgen as mg
-from sympiler_gb300.shard import partition_systems, shard_systems, system_cost
+from sympiler_gb300.shard import column_range, partition_systems, shard_systems, system_cost
 
 
 def _free_port():
@@ -112,3 +112,51 @@ def test_two_gloo_ranks_solve_disjoint_shards(tmp_path):
         orc.sptrsv_csr(L.n, *L.astuple(), x)
         ref.append(x.sum())
     assert np.array_equal(np.load(tmp_path / "sums.npy"), np.array(ref))
+
+
+def _column_worker(rank, world, port, result_dir):
+    """One solve's right-hand-side columns split over the ranks: each rank
+    solves its block against its own copy of the factor (oracle arithmetic
+    on CPU), nothing crosses ranks but the final check's gather."""
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import oracle
+    import torch
+    orc = oracle.orc()
+    L = mg.tril(mg.lap2d(30, 20))
+    k = 7
+    B = np.random.default_rng(21).standard_normal((k, L.n))
+    c0, c1 = column_range(k, rank, world)
+    out = np.zeros((k, L.n))
+    for c in range(c0, c1):
+        x = B[c].copy()
+        orc.sptrsv_csr(L.n, *L.astuple(), x)
+        out[c] = x
+    t = torch.from_numpy(out)
+    dist.all_reduce(t)
+    if rank == 0:
+        np.save(os.path.join(result_dir, "cols.npy"), t.numpy())
+    dist.destroy_process_group()
+
+
+def test_column_ranges_cover_every_column_once():
+    for k in (1, 7, 64, 65):
+        for world in (1, 2, 3, 8):
+            spans = [column_range(k, r, world) for r in range(world)]
+            assert spans[0][0] == 0 and spans[-1][1] == k
+            assert all(spans[r][1] == spans[r + 1][0] for r in range(world - 1))
+            sizes = [b - a for a, b in spans]
+            assert max(sizes) - min(sizes) <= 1
+
+
+def test_two_gloo_ranks_split_the_columns(tmp_path):
+    world = 2
+    mp.spawn(_column_worker, args=(world, _free_port(), str(tmp_path)), nprocs=world, join=True)
+    import oracle
+    orc = oracle.orc()
+    L = mg.tril(mg.lap2d(30, 20))
+    B = np.random.default_rng(21).standard_normal((7, L.n))
+    for c in range(7):
+        orc.sptrsv_csr(L.n, *L.astuple(), B[c])
+    assert np.array_equal(np.load(tmp_path / "cols.npy"), B)
