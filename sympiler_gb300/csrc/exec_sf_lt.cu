@@ -284,17 +284,20 @@ static void lt2_launch(gbsym_tri_s *t, T *x, T *y, const T *bp, cudaStream_t s) 
 
 // ---- several right-hand sides ---------------------------------------------
 // Right-hand sides copied into packed row order (row-major n x k) and the
-// scratch set to the sentinel, in one pass.
+// scratch set to the sentinel, in one pass: a warp per row, its lanes over
+// the row's k values (no division per element).
 template <class T>
 __global__ void k_lt_prep_mrhs(int n, int k, const int *__restrict__ perm, const T *__restrict__ x,
                                T *__restrict__ bp, T *__restrict__ y) {
-  const long long m = (long long)n * k;
-  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < m;
-       e += (long long)gridDim.x * blockDim.x) {
-    const long long row = e / k, c = e - row * k;
-    bp[e] = x[(long long)perm[row] * k + c];
-    if constexpr (sizeof(T) == 8) reinterpret_cast<unsigned long long *>(y)[e] = ~0ull;
-    else reinterpret_cast<unsigned *>(y)[e] = ~0u;
+  const int lane = threadIdx.x & 31;
+  const int nw = (gridDim.x * blockDim.x) >> 5;
+  for (int row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < n; row += nw) {
+    const size_t src = (size_t)perm[row] * k, dst = (size_t)row * k;
+    for (int c = lane; c < k; c += 32) {
+      bp[dst + c] = x[src + c];
+      if constexpr (sizeof(T) == 8) reinterpret_cast<unsigned long long *>(y)[dst + c] = ~0ull;
+      else reinterpret_cast<unsigned *>(y)[dst + c] = ~0u;
+    }
   }
 }
 
@@ -425,8 +428,7 @@ void run_syncfree_lt_mrhs(gbsym_tri_s *t, T *x, int k, cudaStream_t s) {
   t->sfb.reserve(bytes);
   T *y = reinterpret_cast<T *>(t->sfy.p);
   T *bp = reinterpret_cast<T *>(t->sfb.p);
-  const long long m = (long long)t->n * k;
-  const int grid = (int)std::max<long long>(1, std::min<long long>(div_up(m, 256LL), num_sms() * 8LL));
+  const int grid = std::max(1, std::min(div_up(t->n, 8), num_sms() * 8));  // eight warps (rows) per block
   k_lt_prep_mrhs<T><<<grid, 256, 0, s>>>(t->n, k, t->perm.p, x, bp, y);
   check_launch();
   const bool fused = t->arith == kArithFused;
