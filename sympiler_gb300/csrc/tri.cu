@@ -89,8 +89,14 @@ void validate_matrix(int n, const int *d_p, const int *d_i, const int *d_diags, 
 // level of its dependencies (the rule of the reference's build_levelSet_CSC
 // call sites).  Computed by one persistent launch: warps claim 32-row chunks
 // in dependency order from a ticket counter, so every chunk a warp waits on
-// has been claimed by a running warp; inside a chunk the lanes retry in
-// rounds until all 32 rows are resolved.  Waits are bounded.
+// has been claimed by a running warp.  A lane first waits (bounded) for its
+// dependencies in earlier chunks, read from memory as their warps publish
+// them; dependencies inside its own chunk are lower lanes of the same warp
+// and are applied afterwards in one pass of 32 shuffles in lane order (lane
+// s's level is final when the pass reaches it, all its in-chunk
+// dependencies being below it).  A chain of consecutive rows -- the x lines
+// of a grid in natural order -- then costs one shuffle per row instead of a
+// memory round trip.
 __global__ void k_levels_syncfree(int n, const int *__restrict__ p, const int *__restrict__ ci,
                                   const int *__restrict__ diags, int kind, int upper,
                                   int *level, int *ctl /* ticket, err, where, maxlev */) {
@@ -102,7 +108,8 @@ __global__ void k_levels_syncfree(int n, const int *__restrict__ p, const int *_
     if (lane == 0) chunk = atomicAdd(&ctl[0], 1);
     chunk = __shfl_sync(0xffffffffu, chunk, 0);
     if (chunk >= nchunks) break;
-    const int idx = (chunk << 5) + lane;
+    const int base = chunk << 5;
+    const int idx = base + lane;
     const bool active = idx < n;
     const int row = active ? (upper ? n - 1 - idx : idx) : 0;
     int lo = 0, hi = 0;
@@ -112,6 +119,7 @@ __global__ void k_levels_syncfree(int n, const int *__restrict__ p, const int *_
       hi = r.hi;
     }
     int lev = 0, j = lo;
+    unsigned inmask = 0;  // dependencies inside this chunk, as lane bits
     bool done = !active;
     unsigned long long t0 = globaltimer_ns();
     long long iters = 0;
@@ -124,6 +132,13 @@ __global__ void k_levels_syncfree(int n, const int *__restrict__ p, const int *_
             ++j;  // builder kinds: only entries on the dependency side count
             continue;
           }
+          const int cidx = upper ? n - 1 - c : c;
+          if (cidx >= base) {  // a lower lane of this warp: applied by the shuffle pass
+            inmask |= 1u << (cidx - base);
+            ++j;
+            progressed = true;
+            continue;
+          }
           const int lc = ld_relaxed(&level[c]);
           if (lc < 0) break;
           lev = max(lev, lc + 1);
@@ -131,8 +146,6 @@ __global__ void k_levels_syncfree(int n, const int *__restrict__ p, const int *_
           progressed = true;
         }
         if (j >= hi) {
-          st_relaxed(&level[row], lev);
-          my_max = max(my_max, lev);
           done = true;
         } else {
           if (progressed) t0 = globaltimer_ns();
@@ -148,6 +161,14 @@ __global__ void k_levels_syncfree(int n, const int *__restrict__ p, const int *_
     }
     int stop = lane == 0 ? ld_relaxed(&ctl[1]) : 0;
     if (__shfl_sync(0xffffffffu, stop, 0) != 0) break;
+    for (int s = 0; s < 32; ++s) {
+      const int v = __shfl_sync(0xffffffffu, lev, s);
+      if ((inmask >> s) & 1u) lev = max(lev, v + 1);
+    }
+    if (active) {
+      st_relaxed(&level[row], lev);
+      my_max = max(my_max, lev);
+    }
   }
   for (int o = 16; o; o >>= 1) my_max = max(my_max, __shfl_xor_sync(0xffffffffu, my_max, o));
   if (lane == 0 && my_max >= 0) atomicMax(&ctl[3], my_max);
