@@ -1,5 +1,9 @@
-// exec_sf_lt.cu -- the sync-free sweep for one right-hand side with
-// look-through: every row waits on values two levels back instead of one.
+// exec_sf_lt.cu -- the look-through sync-free sweeps: every row recomputes
+// the values it depends on instead of waiting for them, so it waits on
+// values at least two levels back (three for the two-level form) instead
+// of one.  Three forms: one right-hand side over one level (the default
+// where the plan allows it), one right-hand side over two levels, and
+// several right-hand sides over one level (autotuner candidates).
 //
 // With one right-hand side a row takes four lanes of which one computes;
 // here the other three each recompute one of the row's dependencies from
