@@ -143,3 +143,88 @@ def test_several_rhs_lookthrough(gpu, orc, monkeypatch, k, dtype):
                 col = B[:, c].copy()
                 orc.sptrsv_csc(U.n, U.p, U.i, f, col)
                 assert np.array_equal(outs[0][:, c], col)
+
+
+def _random_narrow_lower(n, rng, width):
+    """A random lower triangle whose rows hold 0..3 off-diagonals at random
+    earlier columns (some near, some far), diagonal last: irregular DAGs
+    whose dependencies sit one or many levels back."""
+    import scipy.sparse as sp
+    rows, cols, vals = [], [], []
+    for i in range(1, n):
+        m = int(rng.integers(0, 4))
+        if m == 0:
+            continue
+        near = rng.integers(max(0, i - width), i, size=m)
+        far = rng.integers(0, i, size=m)
+        pick = np.where(rng.uniform(size=m) < 0.7, near, far)
+        for c in np.unique(pick):
+            rows.append(i)
+            cols.append(int(c))
+            vals.append(float(rng.uniform(-1, 1)))
+    d = 2.0 + rng.uniform(0, 1, n)
+    r = np.concatenate([np.asarray(rows, dtype=np.int64), np.arange(n)])
+    c = np.concatenate([np.asarray(cols, dtype=np.int64), np.arange(n)])
+    m = sp.coo_matrix((np.concatenate([vals, d]), (r, c)), shape=(n, n))
+    return mg.from_scipy(m)
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_irregular_dags_all_forms(gpu, orc, monkeypatch, seed):
+    """Random narrow lower triangles: the one-level and two-level one-RHS
+    sweeps and the several-RHS sweep equal the oracle bit for bit."""
+    from sympiler_gb300._lib import EXEC_SYNCFREE
+    from sympiler_gb300.plans import TriPlan
+    rng = np.random.default_rng(seed)
+    L = _random_narrow_lower(int(rng.integers(3000, 12000)), rng, int(rng.integers(2, 200)))
+    b = rng.standard_normal(L.n)
+    ref = b.copy()
+    orc.sptrsv_csr(L.n, *L.astuple(), ref)
+    for levels in (1, 2):
+        P = _plan(monkeypatch, levels, L.n, *L.astuple())
+        assert P.tuning(1)["lookthrough"] == levels
+        assert np.array_equal(_solve(P, b), ref), levels
+    k = 5
+    B = rng.standard_normal((L.n, k))
+    monkeypatch.setenv("GBSYM_SF_LT_MRHS", "1")
+    P = TriPlan(L.n, *L.astuple())
+    monkeypatch.delenv("GBSYM_SF_LT_MRHS")
+    P.set_exec(EXEC_SYNCFREE)
+    assert P.tuning(k)["lookthrough"] == 1
+    X = torch.from_numpy(B.copy()).cuda()
+    P.solve(X)
+    P.check()
+    got = X.cpu().numpy()
+    for c in range(k):
+        col = B[:, c].copy()
+        orc.sptrsv_csr(L.n, *L.astuple(), col)
+        assert np.array_equal(got[:, c], col), c
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 33, 129])
+def test_tiny_and_ragged_systems(gpu, orc, monkeypatch, n):
+    """Systems smaller than a warp unit or one row past it, through the
+    one-level and two-level one-RHS sweeps and the several-RHS sweep."""
+    from sympiler_gb300._lib import EXEC_SYNCFREE
+    from sympiler_gb300.plans import TriPlan
+    rng = np.random.default_rng(n)
+    L = _random_narrow_lower(n, rng, 3)
+    b = rng.standard_normal(n)
+    ref = b.copy()
+    orc.sptrsv_csr(n, *L.astuple(), ref)
+    for levels in (1, 2):
+        P = _plan(monkeypatch, levels, n, *L.astuple())
+        assert np.array_equal(_solve(P, b), ref), levels
+    B = rng.standard_normal((n, 3))
+    monkeypatch.setenv("GBSYM_SF_LT_MRHS", "1")
+    P = TriPlan(n, *L.astuple())
+    monkeypatch.delenv("GBSYM_SF_LT_MRHS")
+    P.set_exec(EXEC_SYNCFREE)
+    X = torch.from_numpy(B.copy()).cuda()
+    P.solve(X)
+    P.check()
+    got = X.cpu().numpy()
+    for c in range(3):
+        col = B[:, c].copy()
+        orc.sptrsv_csr(n, *L.astuple(), col)
+        assert np.array_equal(got[:, c], col), c
