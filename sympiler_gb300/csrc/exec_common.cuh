@@ -27,10 +27,11 @@ enum { kArithExact = 0, kArithFused = 1 };
 // guard stays a branch and only real entries are computed.
 //
 // In FP64 both roundings of the exact update are issued as fused
-// multiply-adds, which this part executes about 19% faster than separate
-// multiplies and adds (measured 597 vs 502 G thread-op/s).  Both forms are
-// bit-identical to the separate operations for every input, signed zeros
-// included:  RN(v*x) = fma(v, x, -0)  (adding -0 changes neither a nonzero
+// multiply-adds with a constant operand; this part runs them at the rate of
+// separate multiplies and subtractions (503 G thread-op/s for either form
+// over all SMs, against 597 for general three-operand FMAs: two DFMAs per SM
+// per clock at most).  Both forms are bit-identical to the separate
+// operations for every input, signed zeros included:  RN(v*x) = fma(v, x, -0)  (adding -0 changes neither a nonzero
 // product nor the sign of a zero one) and  RN(acc - p) = fma(p, -1, acc)
 // (p * -1 is exact, so one rounding of acc - p remains).
 template <int AR, class T>

@@ -241,8 +241,10 @@ namespace gbsym {
 // MODE 0: the exact update acc = RN(acc - RN(v*x)) as the sweeps issue it,
 // MODE 1: general fused multiply-adds with three variable operands (the
 // form of the division's remainder and correction steps).
-// The operands pass through an empty asm each iteration so that no part of
-// an update can be hoisted out of the loop.
+// Every iteration XORs the low mantissa bits of v with the iteration count
+// (integer ops, another pipe), so that no stage of the compiler can hoist
+// the product RN(v*x) out of the loop: an empty asm statement is not
+// enough, as it leaves no instruction behind for the assembler to respect.
 template <int MODE>
 __global__ void __launch_bounds__(256) k_fp64_rate(int iters, double *out) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -256,7 +258,7 @@ __global__ void __launch_bounds__(256) k_fp64_rate(int iters, double *out) {
   for (int it = 0; it < iters; ++it) {
 #pragma unroll
     for (int c = 0; c < 2; ++c) {
-      asm volatile("" : "+d"(x[c]), "+d"(v[c]));
+      v[c] = __longlong_as_double(__double_as_longlong(v[c]) ^ (long long)(it & 1023));
       if (MODE == 0) a[c] = msub<kArithExact>(a[c], v[c], x[c]);
       else a[c] = __fma_rn(__fma_rn(a[c], v[c], x[c]), x[c], v[c]);
     }

@@ -15,10 +15,10 @@ namespace gbsym {
 constexpr int kSpmvRows = 256;
 
 // acc + RN(v * x), both roundings separate (the reference's order), issued
-// in FP64 as fused multiply-adds: RN(v*x) = fma(v, x, -0) and
-// RN(acc + p) = fma(p, 1, acc) are bit-identical to the separate operations
-// for every input, and this part runs DFMA about 19% faster than DMUL/DADD.
-// Inline PTX keeps the compiler from folding them back.
+// in FP64 as fused multiply-adds with a constant operand: RN(v*x) =
+// fma(v, x, -0) and RN(acc + p) = fma(p, 1, acc) are bit-identical to the
+// separate operations for every input, and run at their rate.  Inline PTX
+// keeps the compiler from folding the two into one FMA.
 __device__ __forceinline__ double madd_exact(double acc, double v, double x) {
   double r;
   asm("{\n\t.reg .f64 p;\n\tfma.rn.f64 p, %1, %2, 0d8000000000000000;\n\t"
@@ -30,10 +30,13 @@ __device__ __forceinline__ float madd_exact(float acc, float v, float x) { retur
 
 // MODE 0: y = A x.  MODE 1: z = alpha (z + A x) + beta y.
 // One thread per row, loading its entries directly: on this part the
-// exact FP64 sum is bound by FP64 issue (two FMAs per entry), so the kernel
-// keeps many independent rows in flight with no block barrier in the way;
-// this measured 5-10% faster than staging each block's entries through
-// shared memory.
+// exact FP64 sum is bound by the FP64 pipe (two DFMAs per entry; ncu on the
+// 96^3 convection-diffusion operator: FP64 pipe 72% active, DRAM 36%), so
+// the kernel keeps many independent rows in flight with no barrier in the
+// way.  Staging each block's entries through shared memory measured 5-10%
+// slower; staging each warp's products (coalesced loads, then each lane's
+// ordered sum from shared memory) 29% slower; preloading eight entries per
+// thread before the sum 0-6% slower on that operator.
 template <class T, int MODE>
 __global__ void __launch_bounds__(kSpmvRows)
 k_spmv(int n, const int *__restrict__ p, const int *__restrict__ ci, const T *__restrict__ val,
