@@ -171,3 +171,61 @@ def test_spic0_csr_lbc_drop_in(gpu, orc, parts):
         sym_lib.spic0_csr_lbc(U.n, v, U.p, U.i, 1, np.array([0, 1], np.int32), np.array([0, U.n], np.int32), bad)
     assert e.value.status == ERR_BAD_SCHEDULE
     assert np.array_equal(v, U.x)
+
+
+def _mixed_rows(n, rng):
+    """Rows of 0..12 entries in most warps of 32 rows; a few rows of 40..90
+    entries and a few warps whose 32 rows hold 14 each (more than the 384
+    products a warp stages, so those rows are summed straight from global
+    memory); empty rows; rows whose only product is -0."""
+    import scipy.sparse as sp
+    lens = rng.integers(0, 13, n)
+    wide = rng.choice(n, size=max(1, n // 500), replace=False)
+    lens[wide] = rng.integers(40, 91, wide.size)
+    for w in rng.choice(max(1, n // 32), size=max(1, n // 3000), replace=False):
+        lens[32 * w:32 * w + 32] = 14  # 448 entries in one warp's rows
+    lens[rng.choice(n, size=max(1, n // 50), replace=False)] = 0
+    lens = np.minimum(lens, n)
+    rows = np.repeat(np.arange(n), lens)
+    cols = np.concatenate([np.sort(rng.choice(n, size=l, replace=False)) for l in lens])
+    vals = rng.uniform(-1, 1, rows.size)
+    negz = rng.choice(n, size=max(1, n // 100), replace=False)
+    m = sp.csr_matrix((vals, (rows, cols)), shape=(n, n))
+    m = sp.lil_matrix(m)
+    for r in negz:
+        m.rows[r] = [0]
+        m.data[r] = [-1.0]
+    return mg.from_scipy(sp.csr_matrix(m))
+
+
+@pytest.mark.parametrize("n", [1, 31, 33, 5000, 70001])
+def test_spmv_mixed_rows_signed_zeros_and_axpby(gpu, orc, n):
+    """Warps that stage their products and warps that sum straight from
+    global memory, empty rows, -0 products (0 + -0 = +0), and the
+    accumulate form z = a (z + A x) + b y, bit for bit against the oracle in
+    FP64 and FP32."""
+    from sympiler_gb300.plans import CsrPlan
+    rng = np.random.default_rng(n)
+    A = _mixed_rows(n, rng)
+    v = rng.uniform(-1, 1, n)
+    v[0] = 0.0  # column 0 carries the -1 entries: their product is -0
+    ref = np.zeros(n)
+    orc.spmv_csr(A.n, *A.astuple(), v, ref)
+    P = CsrPlan(A.n, *A.astuple())
+    y = torch.full((n,), 5.0, dtype=torch.float64, device="cuda")
+    P.spmv(torch.from_numpy(v).cuda(), y)
+    got = y.cpu().numpy()
+    assert np.array_equal(got, ref) and np.array_equal(np.signbit(got), np.signbit(ref))
+    yv, z0 = rng.uniform(-1, 1, n), rng.uniform(-1, 1, n)
+    zref = z0.copy()
+    orc.spmv_csr_axpby(A.n, *A.astuple(), v, yv, zref, 0.75, -1.25)
+    z = torch.from_numpy(z0.copy()).cuda()
+    P.spmv_axpby(torch.from_numpy(v).cuda(), torch.from_numpy(yv).cuda(), z, 0.75, -1.25)
+    assert np.array_equal(z.cpu().numpy(), zref)
+    P32 = CsrPlan(A.n, *A.astuple(), dtype="f32")
+    v32 = v.astype(np.float32)
+    ref32 = np.zeros(n, dtype=np.float32)
+    orc.spmv_csr_f32(A.n, A.p, A.i, A.x.astype(np.float32), v32, ref32)
+    y32 = torch.zeros(n, dtype=torch.float32, device="cuda")
+    P32.spmv(torch.from_numpy(v32).cuda(), y32)
+    assert np.array_equal(y32.cpu().numpy(), ref32)
