@@ -174,16 +174,15 @@ def test_spic0_csr_lbc_drop_in(gpu, orc, parts):
 
 
 def _mixed_rows(n, rng):
-    """Rows of 0..12 entries in most warps of 32 rows; a few rows of 40..90
-    entries and a few warps whose 32 rows hold 14 each (more than the 384
-    products a warp stages, so those rows are summed straight from global
-    memory); empty rows; rows whose only product is -0."""
+    """Rows of 0..12 entries; a few rows of 40..90 entries and a few runs of
+    32 rows of 14 entries each (so neighbouring threads' loops run very
+    different lengths); empty rows; rows whose only product is -0."""
     import scipy.sparse as sp
     lens = rng.integers(0, 13, n)
     wide = rng.choice(n, size=max(1, n // 500), replace=False)
     lens[wide] = rng.integers(40, 91, wide.size)
     for w in rng.choice(max(1, n // 32), size=max(1, n // 3000), replace=False):
-        lens[32 * w:32 * w + 32] = 14  # 448 entries in one warp's rows
+        lens[32 * w:32 * w + 32] = 14
     lens[rng.choice(n, size=max(1, n // 50), replace=False)] = 0
     lens = np.minimum(lens, n)
     rows = np.repeat(np.arange(n), lens)
@@ -200,10 +199,9 @@ def _mixed_rows(n, rng):
 
 @pytest.mark.parametrize("n", [1, 31, 33, 5000, 70001])
 def test_spmv_mixed_rows_signed_zeros_and_axpby(gpu, orc, n):
-    """Warps that stage their products and warps that sum straight from
-    global memory, empty rows, -0 products (0 + -0 = +0), and the
-    accumulate form z = a (z + A x) + b y, bit for bit against the oracle in
-    FP64 and FP32."""
+    """Ragged row lengths, empty rows, -0 products (0 + -0 = +0), sizes
+    around one warp, and the accumulate form z = a (z + A x) + b y, bit for
+    bit against the oracle in FP64 and FP32."""
     from sympiler_gb300.plans import CsrPlan
     rng = np.random.default_rng(n)
     A = _mixed_rows(n, rng)
