@@ -610,9 +610,10 @@ int gbsym_batch_get_tuning(gbsym_batch b, int k, int *tuning);
  * is a static device array inside this library (4 MiB per GPU, held until
  * the process exits), so n is limited to 524,288 rows; larger n returns
  * GBSYM_ERR_SIZE without touching x.  The first call on a device does that
- * device's set-up (it looks up the array's address) and should come before
- * any stream capture; calls that overlap on the GPU share the array and
- * race.  Returns when the solve is done (it synchronises `stream`).
+ * device's set-up (it looks up the array's address); calls that overlap on
+ * the GPU share the array and race.  Returns when the solve is done: every
+ * call synchronises `stream` and reads an error word back to the host, so
+ * it cannot be captured into a CUDA graph.
  * Precondition: Lp[0..n] is non-decreasing and Lp[n] lies within Li and
  * Lx -- the kernel reads Li[Lp[i] .. Lp[i+1]) unchecked.  Column indices
  * are checked: one outside [0, i) in row i returns GBSYM_ERR_BAD_MATRIX.

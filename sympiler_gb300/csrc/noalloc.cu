@@ -28,10 +28,10 @@
 // The first call on a device does that device's set-up: it looks up the
 // device address of the static array (cudaGetSymbolAddress, with that
 // device current) and the kernel's resident blocks per SM, and remembers
-// both; make that first call before any stream capture.  Every call
-// clears the part of the array it uses, runs the sweep and copies the
-// error word back, and returns only after the solve has finished on its
-// stream.  All calls share the array and the last call's contents stay in
+// both.  Every call clears the part of the array it uses, runs the sweep
+// and copies the error word back to the host, and returns only after the
+// solve has finished on its stream, so no call can be captured into a CUDA
+// graph.  All calls share the array and the last call's contents stay in
 // it, so calls that overlap on the GPU (different streams, or different
 // host threads on one device) race: serialise them.
 //
