@@ -1,12 +1,17 @@
-"""The one-block executor (one launch, one block, a barrier per level) bit for
-bit against the oracle.
+"""The one-block executor (one launch, one block) bit for bit against the
+oracle, in all three of its forms:
 
-It covers every slab width the pipelined kernel compiles (two, three and four
-entries) and a wider one that keeps the one-level prefetch. It also covers
-one to five levels (the pipeline's partial rounds), levels wider than the
-block (rows past the block's width load their data directly), x in shared
-memory and in global memory, and FP32 and fused arithmetic against the
-sync-free sweep."""
+- barrier-free with values published in shared memory (rows of up to four
+  entries, solution and right-hand side fit in shared memory): the small
+  cases here;
+- level by level with three levels of row data in flight (rows of up to
+  four entries, larger systems): the 30^3 and 200^2 cases;
+- level by level with one level in flight (wider rows): the random case.
+
+It also covers every slab width each form compiles, one to five levels in
+both level-by-level and barrier-free forms, levels wider than the block, x
+in shared memory and in global memory, and FP32 and fused arithmetic
+against the sync-free sweep."""
 import numpy as np
 import pytest
 import scipy.sparse as sp
@@ -44,9 +49,12 @@ def _cases():
     yield "lap3d_20_k3", mg.tril(mg.lap3d(20, 1e-2))
     yield "band_k4", _banded_lower(3000, [1, 2, 40, 41], rng)
     yield "random_wide", mg.random_lower(3000, 0.004, np.random.default_rng(8))
-    for depth in (1, 2, 3, 4, 5):
-        yield "chain_%d_levels" % depth, (mg.from_scipy(sp.eye(600, format="csr") * 2.0) if depth == 1
-                                          else _chain(600, depth, rng))
+    # one to five levels, small (barrier-free form) and, in FP64, too large
+    # for shared memory (the pipelined form's partial rounds)
+    for n in (600, 20000):
+        for depth in (1, 2, 3, 4, 5):
+            yield "chain_%d_%d_levels" % (n, depth), (mg.from_scipy(sp.eye(n, format="csr") * 2.0) if depth == 1
+                                                      else _chain(n, depth, rng))
     yield "lap3d_30_wide_levels", mg.tril(mg.lap3d(30, 1e-2))
     yield "lap2d_200_x_global", mg.tril(mg.lap2d(200))
 
