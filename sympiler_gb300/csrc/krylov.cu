@@ -331,7 +331,7 @@ k_mgs_round(long long n, double *V, long long ld, int k, int mr, double *sc, int
             v[i] = vi;
           }
           if (vnext) sd += vi * q[u];
-          sn += vi * vi;
+          if (want_norm) sn += vi * vi;  // only the passes that report a norm pay for it
         }
       }
     }
