@@ -65,17 +65,22 @@ __device__ __forceinline__ T msub(T acc, T v, T xj) {
 // overflow the remainder or the quotient (and zeros, infinities, NaNs) take
 // IEEE division instead.  Three dependent FP64 operations replace a
 // division that costs about seven FMAs of issue and 280 ns of latency on
-// this part.
+// this part.  The IEEE division is a call out of line: inlined, its code
+// lengthened the common path by about 100 cycles even when not taken (one
+// warp, a dependent chain of divisions: 360 cycles each inlined, 284 out of
+// line, 256 with no range test at all).
+static __device__ __noinline__ double div_ieee(double a, double b) { return __ddiv_rn(a, b); }
 __device__ __forceinline__ double div_by(double a, double b, double y) {
-  const long long ia = __double_as_longlong(a), ib = __double_as_longlong(b);
-  const int ea = (int)((ia >> 52) & 0x7ff), eb = (int)((ib >> 52) & 0x7ff);
-  if (ea >= 63 && ea <= 2043 && eb >= 3 && eb <= 2043 && ea - eb <= 1000 && eb - ea <= 1000) {
-    double q;  // RN(a*y), issued as an FMA (asm: the compiler would fold it back into a multiply)
-    asm("fma.rn.f64 %0, %1, %2, 0d8000000000000000;" : "=d"(q) : "d"(a), "d"(y));
-    const double r = __fma_rn(-q, b, a);
-    return __fma_rn(r, y, q);
-  }
-  return __ddiv_rn(a, b);
+  // biased exponents from the high words; the same ranges as
+  // 63 <= ea <= 2043, 3 <= eb <= 2043, |ea - eb| <= 1000
+  const int ea = (__double2hiint(a) >> 20) & 0x7ff, eb = (__double2hiint(b) >> 20) & 0x7ff;
+  const bool ok = (unsigned)(ea - 63) <= 1980u && (unsigned)(eb - 3) <= 2040u &&
+                  (unsigned)(ea - eb + 1000) <= 2000u;
+  if (__builtin_expect(!ok, 0)) return div_ieee(a, b);
+  double q;  // RN(a*y), issued as an FMA (asm: the compiler would fold it back into a multiply)
+  asm("fma.rn.f64 %0, %1, %2, 0d8000000000000000;" : "=d"(q) : "d"(a), "d"(y));
+  const double r = __fma_rn(-q, b, a);
+  return __fma_rn(r, y, q);
 }
 __device__ __forceinline__ float div_by(float a, float b, float /*y*/) { return __fdiv_rn(a, b); }
 
